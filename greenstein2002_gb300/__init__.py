@@ -1,0 +1,230 @@
+"""GB300-native hot path of the stochastic Greenstein-Winslow myocyte.
+
+Python mirror of the C-ABI in include/gw_fru.h (libgw_fru.so, built in-tree by
+greenstein2002_gb300/build.py).  The compute path is the CUDA library; there
+is no CPU fallback: every call goes through the shared library and raises if
+it is missing or returns an error.
+
+    cell = Cell(nfru=12500)                 # device state of one cell
+    state = cell.init_rest(scheme=0, base=5489)
+    t, states, other, currents = cell.run(state, t=0.0, n_steps=20)
+
+FRU-level operations mirror the reference's MPI layer (mpi_master.c):
+stage() = distrib_simFRU, flux() = send_calc_fru_flux, avg_sums() =
+send_calc_fru_avg, save()/resume() = send_save_state/send_resume_state,
+upload()/download() = initialize_mpi_state/parallel_get_FRUs.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgw_fru.so")
+
+NSTATE, NCUR, NOTHER = 37, 24, 12
+SEED_BASE, SEED_REFERENCE = 0, 1
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+
+
+class GWError(RuntimeError):
+    pass
+
+
+class Settings(C.Structure):
+    """gw_settings of gw_fru.h: the run settings of the reference's
+    parameters.h:92-156 as runtime fields with the same names."""
+    _fields_ = [(n, C.c_double) for n in (
+        "time_start", "time_end", "time_step", "step_min", "step_max", "tolrk",
+        "pulse_duration", "pulse_amplitude", "period", "shift")] + [
+        ("vclamp_flag", C.c_int)] + [(n, C.c_double) for n in (
+            "vclamp_duration", "vclamp_set", "vclamp_shift", "vclamp_hold", "vclamp_period")] + [
+        ("vppclamp_flag", C.c_int)] + [(n, C.c_double) for n in (
+            "vppclamp_ppset", "vppclamp_ppduration", "vppclamp_shift", "vppclamp_set", "vppclamp_duration",
+            "vppclamp_hold", "vppclamp_period")] + [
+        ("iv_flag", C.c_int)] + [(n, C.c_double) for n in (
+            "iv_clamp_duration", "iv_clamp_period", "iv_shift", "iv_clamp_set", "iv_clamp_hold",
+            "iv_clamp_step")] + [
+        ("iv_n", C.c_int), ("chf_flag", C.c_int)] + [(n, C.c_double) for n in (
+            "chfsc_IK1", "chfsc_Jup", "chfsc_INaCa", "chfsc_IKv43", "scale_PCa", "scale_GKr")]
+
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    """Load libgw_fru.so (building it when absent and nvcc is available)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.isfile(LIB_PATH):
+        if not build_if_missing:
+            raise GWError("libgw_fru.so not built: run greenstein2002_gb300/build.py")
+        from . import build as _b
+        _b.build()
+    _lib = bind(LIB_PATH)
+    return _lib
+
+
+def bind(path):
+    """ctypes handle of a library exporting the gw_* native API."""
+    L = C.CDLL(path)
+    P = C.POINTER
+    vp = C.c_void_p
+    sig = {
+        "gw_last_error": ([], C.c_char_p),
+        "gw_create": ([P(vp), C.c_int], C.c_int),
+        "gw_destroy": ([vp], C.c_int),
+        "gw_nfru": ([vp], C.c_int),
+        "gw_set_scale": ([vp, C.c_double], C.c_int),
+        "gw_upload": ([vp, _dp, _ip, _ip, _ip, _ip, _up], C.c_int),
+        "gw_download": ([vp, _dp, _ip, _ip, _ip, _ip, _up], C.c_int),
+        "gw_seed": ([vp, C.c_int, C.c_uint32], C.c_int),
+        "gw_stage": ([vp, C.c_double, C.c_double, _dp, _dp, _dp, _dp], C.c_int),
+        "gw_flux": ([vp, _dp, _dp, _dp], C.c_int),
+        "gw_avg_sums": ([vp, _dp], C.c_int),
+        "gw_save": ([vp], C.c_int),
+        "gw_resume": ([vp], C.c_int),
+        "gw_substeps": ([vp, P(C.c_ulonglong)], C.c_int),
+        "gw_sync": ([vp], C.c_int),
+        "gw_settings_init": ([P(Settings)], None),
+        "gw_rk54pd": ([vp, P(Settings), C.c_double, C.c_double, C.c_double, _dp, _dp, P(C.c_double)], C.c_int),
+        "gw_lastcall": ([vp, P(Settings), C.c_double, _dp, _dp], C.c_int),
+        "gw_run": ([vp, P(Settings), P(C.c_double), _dp, P(C.c_double), C.c_int, vp, vp, vp], C.c_int),
+        "gw_init_rest": ([vp, P(Settings), C.c_int, C.c_uint32, _dp], C.c_int),
+        "gw_dropin_configure": ([C.c_int, C.c_double], None),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name, None)
+        if fn is None:
+            continue
+        fn.argtypes = args
+        fn.restype = res
+    return L
+
+
+def _check(rc, what, L=None):
+    if rc:
+        msg = (L if L is not None else load()).gw_last_error()
+        raise GWError("%s failed (%d): %s" % (what, rc, msg.decode() if msg else ""))
+
+
+def settings(**kw):
+    """Settings with the reference defaults, overridden by keyword."""
+    s = Settings()
+    load().gw_settings_init(C.byref(s))
+    for k, v in kw.items():
+        if not hasattr(s, k):
+            raise KeyError(k)
+        setattr(s, k, v)
+    return s
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Cell:
+    """Device-resident FRU state of one cell (a gw_ctx)."""
+
+    def __init__(self, nfru, nfru_scale=None, lib=None):
+        self._L = L = lib if lib is not None else load()
+        self._h = C.c_void_p()
+        _check(L.gw_create(C.byref(self._h), int(nfru)), "gw_create", self._L)
+        self.nfru = int(nfru)
+        if nfru_scale is not None:
+            _check(L.gw_set_scale(self._h, float(nfru_scale)), "gw_set_scale", self._L)
+
+    def close(self):
+        if self._h:
+            self._L.gw_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- FRU state ----------------------------------------------------------
+    def upload(self, s):
+        n = self.nfru
+        _check(self._L.gw_upload(self._h, np.ascontiguousarray(s["frus"], np.float64).reshape(n * 5),
+                                np.ascontiguousarray(s["ltype"], np.int32).reshape(n * 8),
+                                np.ascontiguousarray(s["ryr"], np.int32).reshape(n * 20),
+                                np.ascontiguousarray(s["ito2"], np.int32).reshape(n * 4),
+                                np.ascontiguousarray(s["mti"], np.int32),
+                                np.ascontiguousarray(s["mt"], np.uint32).reshape(n * 624)), "gw_upload", self._L)
+
+    def download(self):
+        n = self.nfru
+        s = {"frus": np.zeros((n, 5)), "ltype": np.zeros((n, 4, 2), np.int32), "ryr": np.zeros((n, 4, 5), np.int32),
+             "ito2": np.zeros((n, 4), np.int32), "mti": np.zeros(n, np.int32), "mt": np.zeros((n, 624), np.uint32)}
+        _check(self._L.gw_download(self._h, s["frus"].reshape(-1), s["ltype"].reshape(-1), s["ryr"].reshape(-1),
+                                  s["ito2"].reshape(-1), s["mti"], s["mt"].reshape(-1)), "gw_download", self._L)
+        return s
+
+    def seed(self, scheme=SEED_BASE, base=5489):
+        _check(self._L.gw_seed(self._h, int(scheme), int(base) & 0xFFFFFFFF), "gw_seed", self._L)
+
+    # ---- reference MPI-layer operations --------------------------------------
+    def stage(self, t0, tf, dep0, depf):
+        out, num = np.zeros(4), np.zeros(5)
+        _check(self._L.gw_stage(self._h, float(t0), float(tf), np.asarray(dep0, np.float64),
+                               np.asarray(depf, np.float64), out, num), "gw_stage", self._L)
+        return out, num
+
+    def flux(self, dep):
+        out, num = np.zeros(4), np.zeros(5)
+        _check(self._L.gw_flux(self._h, np.asarray(dep, np.float64), out, num), "gw_flux", self._L)
+        return out, num
+
+    def avg_sums(self):
+        num = np.zeros(11)
+        _check(self._L.gw_avg_sums(self._h, num), "gw_avg_sums", self._L)
+        return num
+
+    def save(self):
+        _check(self._L.gw_save(self._h), "gw_save", self._L)
+
+    def resume(self):
+        _check(self._L.gw_resume(self._h), "gw_resume", self._L)
+
+    def substeps(self):
+        c = C.c_ulonglong(0)
+        _check(self._L.gw_substeps(self._h, C.byref(c)), "gw_substeps", self._L)
+        return c.value
+
+    def sync(self):
+        _check(self._L.gw_sync(self._h), "gw_sync", self._L)
+
+    # ---- whole-cell operations -------------------------------------------------
+    def init_rest(self, set_=None, scheme=SEED_BASE, base=5489):
+        state = np.zeros(NSTATE)
+        s = set_ if set_ is not None else settings()
+        _check(self._L.gw_init_rest(self._h, C.byref(s), int(scheme), int(base) & 0xFFFFFFFF, state), "gw_init_rest", self._L)
+        return state
+
+    def rk54pd(self, state, t, tstep, oldstep, set_=None):
+        s = set_ if set_ is not None else settings()
+        cur = np.zeros(NCUR)
+        nxt = C.c_double(0.0)
+        _check(self._L.gw_rk54pd(self._h, C.byref(s), float(t), float(tstep), float(oldstep), state, cur,
+                                C.byref(nxt)), "gw_rk54pd", self._L)
+        return cur, nxt.value
+
+    def run(self, state, t, n_steps, oldstep=None, set_=None, want=("states", "other", "currents")):
+        """Advance n_steps output steps in place; returns (t, states, other, currents)."""
+        s = set_ if set_ is not None else settings()
+        tt = C.c_double(float(t))
+        os_ = C.c_double(float(s.step_max if oldstep is None else oldstep))
+        st = np.zeros((n_steps, NSTATE)) if "states" in want else None
+        ot = np.zeros((n_steps, NOTHER)) if "other" in want else None
+        cu = np.zeros((n_steps, NCUR)) if "currents" in want else None
+        _check(self._L.gw_run(self._h, C.byref(s), C.byref(tt), state, C.byref(os_), int(n_steps), _ptr(st), _ptr(ot),
+                             _ptr(cu)), "gw_run", self._L)
+        self.oldstep = os_.value
+        return tt.value, st, ot, cu

@@ -1,0 +1,303 @@
+// Native C-ABI of the FRU hot path: device memory of one cell, uploads and
+// downloads in the reference's array layout, and the stage / flux / average
+// / save / resume operations that replace the MPI layer of mpi_master.c.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+#include <vector>
+
+#include "gw_fru.h"
+#include "gw_kernels.h"
+#include "gw_fru_model.cuh"
+
+using gw::DevState;
+using gw::StageParams;
+
+static thread_local char g_err[512];
+
+static int set_err(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CK(call)                                                                                \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return set_err(GW_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                          __FILE__, __LINE__);                                  \
+  } while (0)
+
+struct gw_ctx {
+  DevState d;
+  cudaStream_t stream = nullptr;
+  double* h_out = nullptr;  // pinned [32]
+  double nfru_scale = 1.0;
+  uint32_t epoch = 0;
+  int pending = 0;          // kFlagSave / kFlagResume to fold into the next launch
+  int device = 0;
+};
+
+extern "C" const char* gw_last_error(void) { return g_err; }
+
+extern "C" int gw_nfru(const gw_ctx* c) { return c ? c->d.nfru : 0; }
+
+static void free_dev(gw_ctx* c) {
+  void* ptrs[] = {c->d.frus, c->d.chan, c->d.mti, c->d.mt, c->d.frus_s, c->d.chan_s, c->d.mti_s,
+                  c->d.mt_hold, c->d.hold_epoch, c->d.partials, c->d.ticket, c->d.out, c->d.substeps};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+extern "C" int gw_create(gw_ctx** out, int nfru) {
+  if (!out || nfru <= 0) return set_err(GW_EINVAL, "gw_create: nfru must be > 0");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return set_err(GW_ENODEV, "gw_create: no CUDA device available");
+  gw_ctx* c = new (std::nothrow) gw_ctx();
+  if (!c) return set_err(GW_ENOMEM, "gw_create: host allocation failed");
+  cudaGetDevice(&c->device);
+  DevState& d = c->d;
+  d.nfru = nfru;
+  d.stride = (nfru + 31) & ~31;
+  d.nblocks = (nfru + gw::kStageThreads - 1) / gw::kStageThreads;
+  const size_t nf = (size_t)d.stride;
+  cudaError_t e = cudaSuccess;
+#define AL(ptr, bytes) \
+  if (e == cudaSuccess) e = cudaMalloc((void**)&(ptr), (bytes))
+  AL(d.frus, 5 * nf * sizeof(double));
+  AL(d.chan, 4 * nf * sizeof(uint32_t));
+  AL(d.mti, nf * sizeof(int));
+  AL(d.mt, nf * gw::kMtStride * sizeof(uint32_t));
+  AL(d.frus_s, 5 * nf * sizeof(double));
+  AL(d.chan_s, 4 * nf * sizeof(uint32_t));
+  AL(d.mti_s, nf * sizeof(int));
+  AL(d.mt_hold, nf * gw::kMtStride * sizeof(uint32_t));
+  AL(d.hold_epoch, nf * sizeof(uint32_t));
+  AL(d.partials, (size_t)d.nblocks * 16 * sizeof(double));
+  AL(d.ticket, sizeof(unsigned));
+  AL(d.out, 32 * sizeof(double));
+  AL(d.substeps, sizeof(unsigned long long));
+#undef AL
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_out, 32 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.ticket, 0, sizeof(unsigned), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.substeps, 0, sizeof(unsigned long long), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.hold_epoch, 0xff, nf * sizeof(uint32_t), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.frus, 0, 5 * nf * sizeof(double), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.chan, 0, 4 * nf * sizeof(uint32_t), c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    int code = (e == cudaErrorMemoryAllocation) ? GW_ENOMEM : GW_ECUDA;
+    set_err(code, "gw_create(%d): %s", nfru, cudaGetErrorString(e));
+    free_dev(c);
+    delete c;
+    return code;
+  }
+  c->nfru_scale = 12500.0 / (double)nfru;
+  *out = c;
+  return GW_OK;
+}
+
+extern "C" int gw_destroy(gw_ctx* c) {
+  if (!c) return GW_OK;
+  cudaStreamSynchronize(c->stream);
+  free_dev(c);
+  delete c;
+  return GW_OK;
+}
+
+extern "C" int gw_set_scale(gw_ctx* c, double nfru_scale) {
+  if (!c) return set_err(GW_EINVAL, "gw_set_scale: null context");
+  c->nfru_scale = nfru_scale;
+  return GW_OK;
+}
+
+extern "C" int gw_sync(gw_ctx* c) {
+  if (!c) return set_err(GW_EINVAL, "gw_sync: null context");
+  CK(cudaStreamSynchronize(c->stream));
+  return GW_OK;
+}
+
+static int check_states(int n, const int* ltype, const int* ryr, const int* ito2, const int* mti) {
+  for (int f = 0; f < n; f++) {
+    for (int c = 0; c < 4; c++) {
+      int l = ltype[8 * f + 2 * c], v = ltype[8 * f + 2 * c + 1], x = ito2[4 * f + c];
+      if (l < 1 || l > 12 || v < 1 || v > 2 || x < 1 || x > 2)
+        return set_err(GW_EINVAL, "FRU %d cleft %d: channel state out of range (LCC %d, VDI %d, ClCh %d)", f, c, l,
+                       v, x);
+      for (int i = 0; i < 5; i++) {
+        int r = ryr[20 * f + 5 * c + i];
+        if (r < 1 || r > 8) return set_err(GW_EINVAL, "FRU %d cleft %d RyR %d: state %d out of range", f, c, i, r);
+      }
+    }
+    if (mti[f] < 0 || mti[f] > gw::kMtN) return set_err(GW_EINVAL, "FRU %d: mti %d out of range", f, mti[f]);
+  }
+  return GW_OK;
+}
+
+extern "C" int gw_upload(gw_ctx* c, const double* frus, const int* ltype, const int* ryr, const int* ito2,
+                         const int* mti, const uint32_t* mt) {
+  if (!c || !frus || !ltype || !ryr || !ito2 || !mti || !mt) return set_err(GW_EINVAL, "gw_upload: null argument");
+  const int n = c->d.nfru;
+  int rc = check_states(n, ltype, ryr, ito2, mti);
+  if (rc) return rc;
+  const size_t nf = (size_t)c->d.stride;
+  std::vector<double> hf(5 * nf, 0.0);
+  std::vector<uint32_t> hc(4 * nf, 0u);
+  for (int f = 0; f < n; f++) {
+    for (int i = 0; i < 5; i++) hf[i * nf + f] = frus[5 * f + i];
+    for (int k = 0; k < 4; k++) {
+      uint32_t w = (uint32_t)ltype[8 * f + 2 * k] | ((uint32_t)ltype[8 * f + 2 * k + 1] << 4) |
+                   ((uint32_t)ito2[4 * f + k] << 28);
+      for (int i = 0; i < 5; i++) w |= (uint32_t)ryr[20 * f + 5 * k + i] << (8 + 4 * i);
+      hc[k * nf + f] = w;
+    }
+  }
+  CK(cudaMemcpyAsync(c->d.frus, hf.data(), hf.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d.chan, hc.data(), hc.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(c->d.mti, mti, n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpy2DAsync(c->d.mt, gw::kMtStride * sizeof(uint32_t), mt, gw::kMtN * sizeof(uint32_t),
+                       gw::kMtN * sizeof(uint32_t), n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->d.hold_epoch, 0xff, nf * sizeof(uint32_t), c->stream));
+  c->pending = 0;
+  CK(cudaStreamSynchronize(c->stream));  // host staging vectors go out of scope
+  return GW_OK;
+}
+
+// Apply a pending save/resume with a zero-length stage (no substeps).
+static int flush_pending(gw_ctx* c) {
+  if (!c->pending) return GW_OK;
+  StageParams p = {};
+  p.flags = c->pending;
+  p.epoch = c->epoch;
+  p.nfru_scale = c->nfru_scale;
+  c->pending = 0;
+  CK(gw::launch_stage(c->d, p, c->stream));
+  return GW_OK;
+}
+
+extern "C" int gw_download(gw_ctx* c, double* frus, int* ltype, int* ryr, int* ito2, int* mti, uint32_t* mt) {
+  if (!c) return set_err(GW_EINVAL, "gw_download: null context");
+  int rc = flush_pending(c);
+  if (rc) return rc;
+  const int n = c->d.nfru;
+  const size_t nf = (size_t)c->d.stride;
+  std::vector<double> hf(5 * nf);
+  std::vector<uint32_t> hc(4 * nf);
+  CK(cudaMemcpyAsync(hf.data(), c->d.frus, hf.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(hc.data(), c->d.chan, hc.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+  if (mti) CK(cudaMemcpyAsync(mti, c->d.mti, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if (mt)
+    CK(cudaMemcpy2DAsync(mt, gw::kMtN * sizeof(uint32_t), c->d.mt, gw::kMtStride * sizeof(uint32_t),
+                         gw::kMtN * sizeof(uint32_t), n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int f = 0; f < n; f++) {
+    if (frus)
+      for (int i = 0; i < 5; i++) frus[5 * f + i] = hf[i * nf + f];
+    for (int k = 0; k < 4; k++) {
+      const uint32_t w = hc[k * nf + f];
+      if (ltype) {
+        ltype[8 * f + 2 * k] = (int)(w & 15u);
+        ltype[8 * f + 2 * k + 1] = (int)((w >> 4) & 15u);
+      }
+      if (ryr)
+        for (int i = 0; i < 5; i++) ryr[20 * f + 5 * k + i] = (int)((w >> (8 + 4 * i)) & 15u);
+      if (ito2) ito2[4 * f + k] = (int)(w >> 28);
+    }
+  }
+  return GW_OK;
+}
+
+extern "C" int gw_seed(gw_ctx* c, int scheme, uint32_t base) {
+  if (!c || (scheme != gw::kSeedBase && scheme != gw::kSeedReference))
+    return set_err(GW_EINVAL, "gw_seed: bad context or scheme %d", scheme);
+  CK(gw::launch_seed(c->d, scheme, base, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return GW_OK;
+}
+
+static int run_stage(gw_ctx* c, double t0, double tf, const double dep0[3], const double depf[3], int advance,
+                     double out[4], double num[5]) {
+  StageParams p;
+  p.t0 = t0;
+  p.tf = tf;
+  for (int i = 0; i < 3; i++) {
+    p.dep0[i] = dep0[i];
+    p.depf[i] = depf[i];
+    p.span[i] = depf[i] - dep0[i];
+  }
+  p.nfru_scale = c->nfru_scale;
+  p.epoch = c->epoch;
+  p.flags = c->pending | (advance ? gw::kFlagAdvance : 0);
+  c->pending = 0;
+  CK(gw::launch_stage(c->d, p, c->stream));
+  CK(cudaMemcpyAsync(c->h_out, c->d.out, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (num)
+    for (int k = 0; k < 5; k++) num[k] = c->h_out[k];
+  if (out)
+    for (int k = 0; k < 4; k++) out[k] = c->h_out[5 + k];
+  return GW_OK;
+}
+
+extern "C" int gw_stage(gw_ctx* c, double t0, double tf, const double dep0[3], const double depf[3], double out[4],
+                        double num[5]) {
+  if (!c || !dep0 || !depf) return set_err(GW_EINVAL, "gw_stage: null argument");
+  return run_stage(c, t0, tf, dep0, depf, 1, out, num);
+}
+
+extern "C" int gw_flux(gw_ctx* c, const double dep[3], double out[4], double num[5]) {
+  if (!c || !dep) return set_err(GW_EINVAL, "gw_flux: null argument");
+  return run_stage(c, 0.0, 0.0, dep, dep, 0, out, num);
+}
+
+extern "C" int gw_avg_sums(gw_ctx* c, double num[11]) {
+  if (!c || !num) return set_err(GW_EINVAL, "gw_avg_sums: null argument");
+  int rc = flush_pending(c);
+  if (rc) return rc;
+  CK(gw::launch_avg(c->d, c->stream));
+  CK(cudaMemcpyAsync(c->h_out + 16, c->d.out + 16, 11 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < 11; k++) num[k] = c->h_out[16 + k];
+  return GW_OK;
+}
+
+extern "C" int gw_save(gw_ctx* c) {
+  if (!c) return set_err(GW_EINVAL, "gw_save: null context");
+  if (c->pending) {
+    int rc = flush_pending(c);  // a pending resume runs under the old epoch
+    if (rc) return rc;
+  }
+  // A new epoch: the first MT regeneration of each FRU after this point
+  // copies the pre-regeneration words aside (copy-on-twist).
+  c->epoch++;
+  c->pending = gw::kFlagSave;
+  return GW_OK;
+}
+
+extern "C" int gw_resume(gw_ctx* c) {
+  if (!c) return set_err(GW_EINVAL, "gw_resume: null context");
+  if (c->pending) {
+    int rc = flush_pending(c);  // a pending save must land before rolling back to it
+    if (rc) return rc;
+  }
+  c->pending = gw::kFlagResume;
+  return GW_OK;
+}
+
+extern "C" int gw_substeps(gw_ctx* c, unsigned long long* count) {
+  if (!c || !count) return set_err(GW_EINVAL, "gw_substeps: null argument");
+  CK(cudaMemcpyAsync(count, c->d.substeps, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return GW_OK;
+}

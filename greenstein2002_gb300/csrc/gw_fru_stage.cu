@@ -1,0 +1,393 @@
+// FP64 FRU stage kernel: advance every release unit of one cell over one
+// Dormand-Prince stage interval and reduce the fluxes the global ODE needs.
+//
+// Mapping: one thread per FRU (a warp = a group of 32 FRUs).  GB300's FP64
+// rate is ~1/64 of FP32, so FP64 work is the bound and a thread-per-FRU layout
+// keeps every FP64 lane busy with its own FRU instead of replicating per-FRU
+// scalar work across a warp.  FRU state is SoA in HBM (coalesced per warp);
+// each FRU's MT19937 words are one 2560-B row that stays L2-resident (a
+// 12,500-FRU cell holds 32 MB of MT state, well inside the 129 MB L2).
+//
+// Reference: simfru_local.c:32-278 (substep loop), fru_rates_local.c:30-798
+// (rates; inlined in gw_fru_model.cuh), calc_fru_flux_local.c:28-77 and
+// mpi_master.c:401-468 (flux sums and currents), mpi_slave.c:150-226
+// (save/resume of FRU + RNG state for rejected steps).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gw_fru_model.cuh"
+#include "gw_kernels.h"
+
+namespace gw {
+
+// Deterministic block reduction of NV doubles: warp shuffles, then warps in
+// index order.  Result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_reduce(double v[NV], double* smem /* [32][NV] */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; k++) smem[warp * NV + k] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double s = smem[k];
+      for (int w = 1; w < nwarp; w++) s += smem[w * NV + k];
+      v[k] = s;
+    }
+  }
+  __syncthreads();
+}
+
+// Last-block pass: sum the per-block partials in a fixed order, so the result
+// does not depend on which block finished last.  Returns true in thread 0 of
+// the last block, with the totals in tot[].
+template <int NV>
+__device__ __forceinline__ bool grid_finish(const double v[NV], double* partials, unsigned* ticket, double* smem,
+                                            double tot[NV]) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) partials[blockIdx.x * NV + k] = v[k];
+    __threadfence();
+    last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double s[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) s[k] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; k++) s[k] += __ldcg(&partials[b * NV + k]);
+  block_reduce<NV>(s, smem);
+  if (threadIdx.x == 0) {
+    *ticket = 0u;
+#pragma unroll
+    for (int k = 0; k < NV; k++) tot[k] = s[k];
+  }
+  return threadIdx.x == 0;
+}
+
+// Flux numerators -> (Jxfer, Jtr, ICa, Ito2): mpi_master.c:447-468.
+__device__ void currents_from_sums(int nfru, double scale, const double dep[3], const double num[5], double out[4]) {
+  const double V = dep[0], Cai = dep[1], CaNSR = dep[2];
+  const double VFRT = V / RT_over_F, VFsqRT = (1000.0 * Faraday) * VFRT;
+  const double e1 = exp(VFRT), e2 = e1 * e1;
+  double ica, ito2;
+  if (fabs(V) < 1.e-6) {
+    const double icanum = num[2] - num[3] * Cao * 0.341;
+    ica = PCa * 2.0 * 1000.0 * Faraday * icanum;
+    ica = ica / Acap;
+    ito2 = num[4] * PCl * 1000.0 * Faraday * (Clo - Cli);
+    ito2 = ito2 / Acap;
+  } else {
+    const double icanum = num[2] * e2 - num[3] * Cao * 0.341;
+    ica = PCa * 4.0 * VFsqRT * icanum / (e2 - 1.0);
+    ica = ica / Acap;
+    ito2 = num[4] * PCl * VFsqRT * (Cli - Clo * e1) / (1.0 - e1);
+    ito2 = ito2 / Acap;
+  }
+  const double jtr = (((double)nfru) * CaNSR - num[1]) / tautr;
+  const double jxfer = (num[0] - ((double)nfru * (double)kClefts) * Cai) / tauxfer;
+  out[0] = scale * jxfer;
+  out[1] = scale * jtr;
+  out[2] = scale * ica;
+  out[3] = scale * ito2;
+}
+
+// Categorical selection of simfru_local.c:217-226 for a channel that has left
+// its state (u > 1 - dt*total): walk the cumulative probabilities.
+__device__ __forceinline__ int pick_dest(const double r[4], const int d[4], int len, double dt, double u) {
+  double acc = 1.0 - dt * r[0];
+  int n = 1;
+  acc += dt * r[1];
+  while (u > acc && n + 1 < len) {
+    n++;
+    acc += dt * r[n];
+  }
+  return d[n];
+}
+
+// One FRU over [t0, tf]: simfru_local.c:83-277.
+__device__ __forceinline__ void advance_fru(const StageParams& p, double y[5], uint32_t w[kClefts], MtRef& rng,
+                                            uint32_t& nsub) {
+  double dep[3], lopen[kClefts], R0[32];
+  int nopen[kClefts];
+#pragma unroll
+  for (int i = 0; i < 3; i++) dep[i] = p.dep0[i];
+#pragma unroll
+  for (int c = 0; c < kClefts; c++) {
+    lopen[c] = lcc_open(w[c]) ? 1.0 : 0.0;
+    nopen[c] = ryr_open_count(w[c]);
+  }
+  const double interval = p.tf - p.t0;
+  double t = p.t0;
+  while (t < p.tf) {
+    // ---- exit rates at the substep start (fru_rates_local.c:126-777) ----
+    const LccBasis lb = lcc_basis(dep[0]);
+    const double nu = 1.0;
+    const double yinf = nu * (0.4 / (1.0 + exp((dep[0] + 12.5) / 5.0)) + (1.0 - 0.4));
+    const double tau = 60.0 + 340.0 / (1.0 + exp((dep[0] + 30.0) / 12.0));
+    const double vdi_open_rate = (1.0 - yinf) / tau, vdi_closed_rate = yinf / tau;
+    double cass0[kClefts];
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) {
+      cass0[c] = y[c + 1];
+      R0[8 * c + 0] = lcc_total(lcc_of(w[c]), lb, gammacf * y[c + 1]);
+      R0[8 * c + 1] = (vdi_of(w[c]) == 2) ? vdi_open_rate : vdi_closed_rate;
+    }
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) {
+      const RyrK k = ryr_constants(y[c + 1]);
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) {
+        const int s = ryr_resolve(ryr_of(w[c], i), k, rng);
+        w[c] = set_field(w[c], 8 + 4 * i, s);
+        R0[8 * c + 2 + i] = ryr_total(s, k);
+      }
+      R0[8 * c + 7] = (cl_of(w[c]) == 1) ? kfIto2 * y[c + 1] : kbIto2;
+    }
+    double mx = 0.0;
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) {
+      mx = dmax(mx, R0[8 * c + 0]);
+      mx = dmax(mx, R0[8 * c + 1]);
+      mx = dmax(mx, R0[8 * c + 7]);
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) mx = dmax(mx, R0[8 * c + 2 + i]);
+    }
+    // ---- substep size (simfru_local.c:135-146) ----
+    double dt = dmin(0.1 / mx, 10.001e-3);
+    double cmax = 0.e-3;
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) cmax = dmax(cmax, y[c + 1]);
+    if (cmax > 1.5e-3) dt = dmin(dt, 5.001e-3);
+    dt = dmin(dt, p.tf - t);
+    // ---- Heun step of the local Ca ODE with pre-transition flags (:149-173) ----
+    double k1[5], y1[5], dF[5];
+    fcn_fru(y, dep, lopen, nopen, dF);
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+      k1[i] = dt * dF[i];
+      y1[i] = y[i] + k1[i];
+    }
+    t = t + dt;
+#pragma unroll
+    for (int i = 0; i < 3; i++) dep[i] = p.dep0[i] + (t - p.t0) / interval * p.span[i];
+    fcn_fru(y1, dep, lopen, nopen, dF);
+#pragma unroll
+    for (int i = 0; i < 5; i++) y[i] = y[i] + (k1[i] + dt * dF[i]) / 2.0;
+    // ---- 32 uniforms and transitions (:211-276) ----
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) {
+      bool moved = false;
+      // LCC
+      {
+        const double u = rng.next();
+        if (u > 1.0 - dt * R0[8 * c]) {
+          double r[4];
+          int d[4];
+          const int len = lcc_row(lcc_of(w[c]), lb, gammacf * cass0[c], r, d);
+          w[c] = set_field(w[c], 0, pick_dest(r, d, len, dt, u));
+        }
+      }
+      // voltage-dependent inactivation gate
+      {
+        const double u = rng.next();
+        if (u >= 1.0 - dt * R0[8 * c + 1]) w[c] = set_field(w[c], 4, 3 - vdi_of(w[c]));
+      }
+      // RyRs
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) {
+        const double u = rng.next();
+        if (u > 1.0 - dt * R0[8 * c + 2 + i]) {
+          const RyrK k = ryr_constants(cass0[c]);
+          double r[4];
+          int d[4];
+          const int len = ryr_row(ryr_of(w[c], i), k, r, d);
+          w[c] = set_field(w[c], 8 + 4 * i, pick_dest(r, d, len, dt, u));
+          moved = true;
+        }
+      }
+      // Ca-activated Cl channel
+      {
+        const double u = rng.next();
+        if (u >= 1.0 - dt * R0[8 * c + 7]) w[c] = set_field(w[c], 28, 3 - cl_of(w[c]));
+      }
+      lopen[c] = lcc_open(w[c]) ? 1.0 : 0.0;
+      if (moved) nopen[c] = ryr_open_count(w[c]);
+    }
+    nsub++;
+  }
+}
+
+__global__ void __launch_bounds__(kStageThreads) fru_stage_kernel(DevState s, StageParams p) {
+  __shared__ double smem[32 * 5];
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  uint32_t nsub = 0;
+  if (f < s.nfru) {
+    const size_t nf = (size_t)s.stride;
+    double y[5];
+    uint32_t w[kClefts];
+    int mti;
+    MtRef rng;
+    rng.m = s.mt + (size_t)f * kMtStride;
+    rng.hold = s.mt_hold + (size_t)f * kMtStride;
+    rng.hold_epoch = s.hold_epoch + f;
+    rng.epoch = p.epoch;
+    if (p.flags & kFlagResume) {
+      // mpi_slave.c:150-184: back to the saved FRU and RNG state
+#pragma unroll
+      for (int i = 0; i < 5; i++) y[i] = s.frus_s[i * nf + f];
+#pragma unroll
+      for (int c = 0; c < kClefts; c++) w[c] = s.chan_s[c * nf + f];
+      mti = s.mti_s[f];
+      if (*rng.hold_epoch == p.epoch)
+        for (int k = 0; k < kMtN; k++) rng.m[k] = rng.hold[k];
+    } else {
+#pragma unroll
+      for (int i = 0; i < 5; i++) y[i] = s.frus[i * nf + f];
+#pragma unroll
+      for (int c = 0; c < kClefts; c++) w[c] = s.chan[c * nf + f];
+      mti = s.mti[f];
+    }
+    if (p.flags & kFlagSave) {
+      // mpi_slave.c:192-226: snapshot; the MT words are protected lazily by
+      // copy-on-twist under the new epoch
+#pragma unroll
+      for (int i = 0; i < 5; i++) s.frus_s[i * nf + f] = y[i];
+#pragma unroll
+      for (int c = 0; c < kClefts; c++) s.chan_s[c * nf + f] = w[c];
+      s.mti_s[f] = mti;
+    }
+    rng.mti = mti;
+    if (p.flags & kFlagAdvance) advance_fru(p, y, w, rng, nsub);
+#pragma unroll
+    for (int i = 0; i < 5; i++) s.frus[i * nf + f] = y[i];
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) s.chan[c * nf + f] = w[c];
+    s.mti[f] = rng.mti;
+    // flux numerators of this FRU (calc_fru_flux_local.c:45-70)
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) {
+      v[0] += y[c + 1];
+      if (lcc_open(w[c])) {
+        v[2] += y[c + 1];
+        v[3] += 1.0;
+      }
+      if (cl_of(w[c]) == 2) v[4] += 1.0;
+    }
+    v[1] = y[0];
+  }
+  if (s.substeps) {
+    // substep counter (workload accounting): warp-aggregated atomic
+    unsigned long long c = nsub;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(s.substeps, c);
+  }
+  block_reduce<5>(v, smem);
+  double tot[5];
+  if (grid_finish<5>(v, s.partials, s.ticket, smem, tot)) {
+    double cur[4];
+    currents_from_sums(s.nfru, p.nfru_scale, p.depf, tot, cur);
+#pragma unroll
+    for (int k = 0; k < 5; k++) s.out[k] = tot[k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) s.out[5 + k] = cur[k];
+  }
+}
+
+// Output-cadence sums of calc_fru_avg_local.c:27-105 (11 values).
+__global__ void __launch_bounds__(kStageThreads) fru_avg_kernel(DevState s) {
+  __shared__ double smem[32 * 11];
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[11];
+#pragma unroll
+  for (int k = 0; k < 11; k++) v[k] = 0.0;
+  if (f < s.nfru) {
+    const size_t nf = (size_t)s.stride;
+    const double jsr = s.frus[f];
+    v[1] = jsr;
+    v[6] = jsr * (1.0 + CSQNtot / (KmCSQN + jsr));
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) {
+      const double ss = s.frus[(c + 1) * nf + f];
+      const uint32_t w = s.chan[c * nf + f];
+      int no = 0, ready = 0;
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) {
+        const int r = ryr_of(w, i);
+        no += ryr_open(r);
+        ready += (r == 1 || r == 2);
+      }
+      v[0] += ss;
+      v[5] += ss * (1.0 + BSRtot / (KBSR + ss) + BSLtot / (KBSL + ss));
+      v[2] += JRyRmax * ((double)no) * (jsr - ss);
+      v[3] += (double)no;
+      v[4] += (double)ready;
+      if (lcc_of(w) <= 6) v[7] += 1.0;
+      if (vdi_of(w) == 2) v[8] += 1.0;
+      if (lcc_open(w)) v[9] += 1.0;
+      if (cl_of(w) == 2) v[10] += 1.0;
+    }
+  }
+  block_reduce<11>(v, smem);
+  double tot[11];
+  if (grid_finish<11>(v, s.partials, s.ticket, smem, tot))
+#pragma unroll
+    for (int k = 0; k < 11; k++) s.out[16 + k] = tot[k];
+}
+
+// Knuth initialisation of every FRU's MT19937 state (mt19937_local.c:76-92),
+// seeded either by base + j or by the formula of initialize_ran.c:30-34.
+__global__ void fru_seed_kernel(DevState s, int scheme, uint32_t base) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= s.nfru) return;
+  uint32_t seed;
+  if (scheme == kSeedReference) {
+    // a_j = 12350232 + 23*(0+1+..+j); seed = |a_j + 4093*j*j| + 1 in 32-bit
+    // two's-complement arithmetic
+    const uint32_t j = (uint32_t)f;
+    const uint32_t tri = (uint32_t)(((uint64_t)j * (uint64_t)(j + 1)) / 2u);
+    const uint32_t a = 12350232u + 23u * tri;
+    int32_t t = (int32_t)(a + (4093u * j) * j);
+    if (t < 0) t = (int32_t)(0u - (uint32_t)t);
+    seed = (uint32_t)t + 1u;
+  } else {
+    seed = base + (uint32_t)f;
+  }
+  uint32_t* m = s.mt + (size_t)f * kMtStride;
+  uint32_t x = seed;
+  m[0] = x;
+  for (uint32_t i = 1; i < kMtN; i++) {
+    x = 1812433253u * (x ^ (x >> 30)) + i;
+    m[i] = x;
+  }
+  s.mti[f] = kMtN;
+  s.hold_epoch[f] = 0xffffffffu;
+}
+
+}  // namespace gw
+
+// ---- launchers (C++ linkage, used by gw_abi.cu) -------------------------------
+namespace gw {
+cudaError_t launch_stage(const DevState& s, const StageParams& p, cudaStream_t st) {
+  fru_stage_kernel<<<s.nblocks, kStageThreads, 0, st>>>(s, p);
+  return cudaGetLastError();
+}
+cudaError_t launch_avg(const DevState& s, cudaStream_t st) {
+  fru_avg_kernel<<<s.nblocks, kStageThreads, 0, st>>>(s);
+  return cudaGetLastError();
+}
+cudaError_t launch_seed(const DevState& s, int scheme, uint32_t base, cudaStream_t st) {
+  fru_seed_kernel<<<s.nblocks, kStageThreads, 0, st>>>(s, scheme, base);
+  return cudaGetLastError();
+}
+}  // namespace gw

@@ -1,0 +1,54 @@
+// Device-state layout and kernel launchers shared by the CUDA sources.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gw {
+
+constexpr int kStageThreads = 128;
+
+enum : int {
+  kFlagAdvance = 1,  // run the substep loop over [t0, tf]
+  kFlagSave = 2,     // snapshot FRU state before advancing (send_save_state)
+  kFlagResume = 4,   // restore the snapshot before advancing (send_resume_state)
+};
+enum : int { kSeedBase = 0, kSeedReference = 1 };
+
+// Device arrays of one cell.  SoA with row stride `stride` (>= nfru):
+//   frus[5][stride]   CaJSR, CaSS1..4 (mM)
+//   chan[4][stride]   packed channel states of each cleft (gw_fru_model.cuh)
+//   mti[stride], mt[nfru][640] (FRU-major MT19937 rows)
+//   *_s               snapshot taken at the last save
+//   mt_hold/hold_epoch  copy-on-twist protection of the saved MT words
+//   partials[nblocks][16], ticket: scratch of the deterministic grid reduction
+//   out[32]           [0..4] flux sums, [5..8] Jxfer,Jtr,ICa,Ito2, [16..26] averages
+struct DevState {
+  int nfru, stride, nblocks;
+  double* frus;
+  uint32_t* chan;
+  int* mti;
+  uint32_t* mt;
+  double* frus_s;
+  uint32_t* chan_s;
+  int* mti_s;
+  uint32_t* mt_hold;
+  uint32_t* hold_epoch;
+  double* partials;
+  unsigned* ticket;
+  double* out;
+  unsigned long long* substeps;
+};
+
+struct StageParams {
+  double t0, tf;
+  double dep0[3], span[3], depf[3];
+  double nfru_scale;
+  uint32_t epoch;
+  int flags;
+};
+
+cudaError_t launch_stage(const DevState& s, const StageParams& p, cudaStream_t st);
+cudaError_t launch_avg(const DevState& s, cudaStream_t st);
+cudaError_t launch_seed(const DevState& s, int scheme, uint32_t base, cudaStream_t st);
+
+}  // namespace gw

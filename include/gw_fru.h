@@ -1,0 +1,164 @@
+/*
+ * gw_fru.h -- C-ABI of the GB300 FRU hot path (libgw_fru.so).
+ *
+ * Two layers, both plain C (no CUDA or torch types in any signature):
+ *
+ *  1. The drop-in layer: the FRU-distribution entry points of the reference's
+ *     MPI layer with their exact names and signatures (declared in the
+ *     reference's parameters.h:255-271).  A program built from the reference's
+ *     caf.c / rk_pd54m.c / fcn.c links against this library instead of
+ *     mpi_master.c + mpi_slave.c and runs its FRUs on the GPU.  Each call
+ *     aborts with a message on a CUDA error, as the reference aborts on I/O
+ *     errors.  NFRU_sim and NFRU_scale are read from the program's globals
+ *     (caf.c:34-36) when it defines them, else from gw_dropin_configure().
+ *
+ *  2. The native layer (gw_*): explicit context, runtime settings, int status
+ *     codes, multi-cell capable.  The drop-in layer is built on it.
+ *
+ * Array layouts are the reference's: per FRU ltype[4][2], ryr[4][5], ito2[4],
+ * frus[5] (CaJSR, CaSS1..4), mti, and 624 MT19937 state words.
+ */
+#ifndef GW_FRU_H
+#define GW_FRU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------- */
+/* Status codes                                                               */
+/* ------------------------------------------------------------------------- */
+#define GW_OK 0
+#define GW_EINVAL 1     /* bad argument (size, pointer, state value) */
+#define GW_ECUDA 2      /* CUDA runtime error (message via gw_last_error) */
+#define GW_ENOMEM 3     /* device or host allocation failed */
+#define GW_ENODEV 4     /* no usable GPU */
+
+const char *gw_last_error(void);
+
+/* ------------------------------------------------------------------------- */
+/* Native layer                                                               */
+/* ------------------------------------------------------------------------- */
+typedef struct gw_ctx gw_ctx;
+
+/* Cell of nfru FRUs on the current CUDA device (replaces the per-rank FRU
+ * blocks of initialize_mpi_state, mpi_master.c:199-361). */
+int gw_create(gw_ctx **ctx, int nfru);
+int gw_destroy(gw_ctx *ctx);
+int gw_nfru(const gw_ctx *ctx);
+
+/* Flux scale factor 12500/NFRU (parameters.h:43-46) and the LCC
+ * permeability scale (1.0 = reference PCa, parameters_fcn_fru.c:48). */
+int gw_set_scale(gw_ctx *ctx, double nfru_scale);
+
+/* FRU state upload / download (host arrays in the reference layout; mt as
+ * uint32 words [n][624]).  Replace the scatter of initialize_mpi_state
+ * (mpi_master.c:199) and the gather of parallel_get_FRUs (mpi_master.c:509). */
+int gw_upload(gw_ctx *ctx, const double *frus, const int *ltype, const int *ryr, const int *ito2, const int *mti,
+              const uint32_t *mt);
+int gw_download(gw_ctx *ctx, double *frus, int *ltype, int *ryr, int *ito2, int *mti, uint32_t *mt);
+
+/* Seed every FRU's MT19937 on the device: scheme 0 = seed base+j,
+ * scheme 1 = the formula of initialize_ran.c:30-34. */
+int gw_seed(gw_ctx *ctx, int scheme, uint32_t base);
+
+/* One Dormand-Prince stage: advance all FRUs over [t0, tf] with V/Cai/CaNSR
+ * interpolated from dep0 to depf; out = Jxfer, Jtr, ICa, Ito2 at depf.
+ * num (optional, may be NULL) receives the 5 flux numerators.
+ * Replaces distrib_simFRU (mpi_master.c:369-469). */
+int gw_stage(gw_ctx *ctx, double t0, double tf, const double dep0[3], const double depf[3], double out[4],
+             double num[5]);
+/* Fluxes of the current FRU state at dep (send_calc_fru_flux, mpi_master.c:41). */
+int gw_flux(gw_ctx *ctx, const double dep[3], double out[4], double num[5]);
+/* The 11 output sums of calc_fru_avg_local.c:27 (send_calc_fru_avg). */
+int gw_avg_sums(gw_ctx *ctx, double num[11]);
+/* Snapshot / rollback of FRU + RNG state (send_save_state :477,
+ * send_resume_state :493).  Applied lazily by the next device operation. */
+int gw_save(gw_ctx *ctx);
+int gw_resume(gw_ctx *ctx);
+
+/* FRU-substeps executed since creation (workload counter). */
+int gw_substeps(gw_ctx *ctx, unsigned long long *count);
+/* Wait for all work of the context. */
+int gw_sync(gw_ctx *ctx);
+
+/* Run settings of parameters.h:92-156 as a runtime struct; see
+ * gw_protocol_init for the defaults (the reference's parameters.h values). */
+typedef struct gw_settings {
+  double time_start, time_end, time_step, step_min, step_max, tolrk;
+  double pulse_duration, pulse_amplitude, period, shift;
+  int vclamp_flag;
+  double vclamp_duration, vclamp_set, vclamp_shift, vclamp_hold, vclamp_period;
+  int vppclamp_flag;
+  double vppclamp_ppset, vppclamp_ppduration, vppclamp_shift, vppclamp_set, vppclamp_duration, vppclamp_hold,
+      vppclamp_period;
+  int iv_flag;
+  double iv_clamp_duration, iv_clamp_period, iv_shift, iv_clamp_set, iv_clamp_hold, iv_clamp_step;
+  int iv_n;
+  int chf_flag;
+  double chfsc_IK1, chfsc_Jup, chfsc_INaCa, chfsc_IKv43;
+  double scale_PCa, scale_GKr;
+} gw_settings;
+
+void gw_settings_init(gw_settings *s);
+
+/* Adaptive Dormand-Prince 5(4) over [t, tstep] with FRU stages on the GPU
+ * (rk_pd54m.c:29-345).  state[37] in/out, current[24] out; returns the step
+ * size to start the next call with in *next_step. */
+int gw_rk54pd(gw_ctx *ctx, const gw_settings *set, double t, double tstep, double oldstepsize, double *state,
+              double *current, double *next_step);
+/* Final currents at `time` (fcn.c:1077). */
+int gw_lastcall(gw_ctx *ctx, const gw_settings *set, double time, double *state, double *current);
+
+/* Whole-cell run: n_steps output steps of set->time_step from *t (the main
+ * loop of caf.c:150-251).  Per step k it stores states[k][37] at t+(k+1)dt,
+ * other[k][12] (otherstates), currents[k][24] at t+k*dt; any of them may be
+ * NULL.  *t, state, *oldstep advance in place. */
+int gw_run(gw_ctx *ctx, const gw_settings *set, double *t, double *state, double *oldstep, int n_steps,
+           double *states, double *other, double *currents);
+
+/* Rest initial conditions of initialize_state.c:164-246 for the cell:
+ * 37 globals (CaTOT from the FRU sums) and every FRU at rest, seeded by
+ * `scheme`/`base` as in gw_seed. */
+int gw_init_rest(gw_ctx *ctx, const gw_settings *set, int scheme, uint32_t base, double *state);
+
+/* ------------------------------------------------------------------------- */
+/* Drop-in layer: reference names and signatures (parameters.h:255-271).      */
+/* ------------------------------------------------------------------------- */
+/* Overrides for programs that do not define the globals NFRU_sim and
+ * NFRU_scale of caf.c:34-36. */
+void gw_dropin_configure(int nfru, double nfru_scale);
+/* The context the drop-in layer uses (created by initialize_mpi_state). */
+gw_ctx *gw_dropin_context(void);
+
+/* mpi_master.c:625 -- sets *rank = 0, *procs = 1 (one GPU, one process). */
+void initialize_mpi(int *argc, char **argv, int *rank, int *procs);
+/* mpi_master.c:643 -- releases the GPU context. */
+void end_mpi(void);
+/* mpi_master.c:199 -- uploads the first NFRU_sim FRUs.  mt rows are the
+ * reference's unsigned long[625] arrays. */
+void initialize_mpi_state(double FRU_states[][5], int LType_state[][4][2], int RyR_state[][4][5],
+                          int Ito2_state[][4], int mti[], unsigned long mt[][625]);
+/* mpi_master.c:369 */
+void distrib_simFRU(double st_time, double end_time, double FRUdep_states0[3], double FRUdep_statesf[3],
+                    double *Jxfer, double *Jtr, double *ICa, double *Ito2);
+/* mpi_master.c:41 */
+void send_calc_fru_flux(double FRUdep_states[3], double *Jxfer, double *Jtr, double *ICa, double *Ito2);
+/* mpi_master.c:122 -- otherstate[12] from the FRU sums and state[37]. */
+void send_calc_fru_avg(double state[37], double otherstate[12]);
+/* mpi_master.c:477, :493 */
+void send_save_state(void);
+void send_resume_state(void);
+/* mpi_master.c:509 -- downloads all FRUs into the reference's arrays. */
+void parallel_get_FRUs(double FRU_states[][5], int LType_state[][4][2], int RyR_state[][4][5], int Ito2_state[][4],
+                       unsigned long mt[][625], int mti[]);
+/* mpi_slave.c:348 -- the worker loop; never entered with one process. */
+void parallel(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GW_FRU_H */
