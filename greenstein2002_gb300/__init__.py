@@ -96,6 +96,13 @@ def bind(path):
         "gw_run": ([vp, P(Settings), P(C.c_double), _dp, P(C.c_double), C.c_int, vp, vp, vp], C.c_int),
         "gw_init_rest": ([vp, P(Settings), C.c_int, C.c_uint32, _dp], C.c_int),
         "gw_dropin_configure": ([C.c_int, C.c_double], None),
+        "gw_event_record": ([vp, C.c_int], C.c_int),
+        "gw_event_elapsed": ([vp, C.c_int, C.c_int, P(C.c_float)], C.c_int),
+        "gw_profile": ([vp, C.c_int], C.c_int),
+        "gw_profile_read": ([vp, P(C.c_double), P(C.c_ulonglong)], C.c_int),
+        "gw_launches": ([vp, P(C.c_ulonglong)], C.c_int),
+        "gw_l2_flush": ([vp], C.c_int),
+        "gw_probe_fp64_peak": ([P(C.c_double)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name, None)
@@ -198,6 +205,30 @@ class Cell:
         _check(self._L.gw_substeps(self._h, C.byref(c)), "gw_substeps", self._L)
         return c.value
 
+    def event(self, slot):
+        _check(self._L.gw_event_record(self._h, int(slot)), "gw_event_record", self._L)
+
+    def elapsed_ms(self, a, b):
+        ms = C.c_float(0.0)
+        _check(self._L.gw_event_elapsed(self._h, int(a), int(b), C.byref(ms)), "gw_event_elapsed", self._L)
+        return ms.value
+
+    def profile(self, enable=True):
+        _check(self._L.gw_profile(self._h, 1 if enable else 0), "gw_profile", self._L)
+
+    def profile_read(self):
+        ms, n = C.c_double(0.0), C.c_ulonglong(0)
+        _check(self._L.gw_profile_read(self._h, C.byref(ms), C.byref(n)), "gw_profile_read", self._L)
+        return ms.value, n.value
+
+    def launches(self):
+        n = C.c_ulonglong(0)
+        _check(self._L.gw_launches(self._h, C.byref(n)), "gw_launches", self._L)
+        return n.value
+
+    def l2_flush(self):
+        _check(self._L.gw_l2_flush(self._h), "gw_l2_flush", self._L)
+
     def sync(self):
         _check(self._L.gw_sync(self._h), "gw_sync", self._L)
 
@@ -228,3 +259,10 @@ class Cell:
                              _ptr(cu)), "gw_run", self._L)
         self.oldstep = os_.value
         return tt.value, st, ot, cu
+
+
+def fp64_peak_tflops():
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    v = C.c_double(0.0)
+    _check(load().gw_probe_fp64_peak(C.byref(v)), "gw_probe_fp64_peak")
+    return v.value

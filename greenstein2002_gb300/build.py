@@ -15,6 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 INC = os.path.join(os.path.dirname(HERE), "include")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgw_fru.so")
+EXE = os.path.join(OUT, "gw_caf")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -23,6 +24,7 @@ CUDA_UNITS = {
     # source: extra flags
     "gw_fru_stage.cu": ["-fmad=false"],
     "gw_abi.cu": [],
+    "gw_probe.cu": [],
 }
 C_UNITS = ["gw_dp.c", "gw_dropin.c"]
 
@@ -35,11 +37,12 @@ def _nvcc():
 
 
 def _sources():
-    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INC, "gw_fru.h")]
+    return ([os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INC, "gw_fru.h")] +
+            [os.path.join(HERE, "host", f) for f in os.listdir(os.path.join(HERE, "host"))])
 
 
 def up_to_date():
-    if not os.path.isfile(LIB):
+    if not os.path.isfile(LIB) or not os.path.isfile(EXE):
         return False
     t = os.path.getmtime(LIB)
     return all(os.path.getmtime(s) <= t for s in _sources())
@@ -76,6 +79,9 @@ def build(force=False, verbose=False):
             if verbose and out.strip():
                 print(out)
     run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lm"])
+    # the C host driver (caf.c main loop) linked against the library
+    run([cc, "-O2", "-std=c99", "-ffp-contract=off", "-Wall", "-I" + CSRC, "-I" + INC, "-o", EXE,
+         os.path.join(HERE, "host", "gw_caf.c"), "-L" + OUT, "-lgw_fru", "-Wl,-rpath,$ORIGIN", "-lm"])
     return LIB
 
 

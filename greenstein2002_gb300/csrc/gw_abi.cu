@@ -43,6 +43,12 @@ struct gw_ctx {
   uint32_t epoch = 0;
   int pending = 0;          // kFlagSave / kFlagResume to fold into the next launch
   int device = 0;
+  cudaEvent_t ev[8] = {};
+  cudaEvent_t pev[2] = {};  // bracket of the last stage launch while profiling
+  bool profiling = false;
+  double prof_ms = 0.0;
+  unsigned long long prof_launches = 0, launches = 0;
+  void* flush_buf = nullptr;
 };
 
 extern "C" const char* gw_last_error(void) { return g_err; }
@@ -55,6 +61,11 @@ static void free_dev(gw_ctx* c) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->flush_buf) cudaFree(c->flush_buf);
+  for (cudaEvent_t e : c->ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->pev)
+    if (e) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -90,7 +101,10 @@ extern "C" int gw_create(gw_ctx** out, int nfru) {
 #undef AL
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_out, 32 * sizeof(double));
+  for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
+  for (int i = 0; i < 2 && e == cudaSuccess; i++) e = cudaEventCreate(&c->pev[i]);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.ticket, 0, sizeof(unsigned), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.out, 0, 32 * sizeof(double), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.substeps, 0, sizeof(unsigned long long), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.hold_epoch, 0xff, nf * sizeof(uint32_t), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.frus, 0, 5 * nf * sizeof(double), c->stream);
@@ -183,6 +197,7 @@ static int flush_pending(gw_ctx* c) {
   p.nfru_scale = c->nfru_scale;
   c->pending = 0;
   CK(gw::launch_stage(c->d, p, c->stream));
+  c->launches++;
   return GW_OK;
 }
 
@@ -222,6 +237,7 @@ extern "C" int gw_seed(gw_ctx* c, int scheme, uint32_t base) {
   if (!c || (scheme != gw::kSeedBase && scheme != gw::kSeedReference))
     return set_err(GW_EINVAL, "gw_seed: bad context or scheme %d", scheme);
   CK(gw::launch_seed(c->d, scheme, base, c->stream));
+  c->launches++;
   CK(cudaStreamSynchronize(c->stream));
   return GW_OK;
 }
@@ -240,9 +256,24 @@ static int run_stage(gw_ctx* c, double t0, double tf, const double dep0[3], cons
   p.epoch = c->epoch;
   p.flags = c->pending | (advance ? gw::kFlagAdvance : 0);
   c->pending = 0;
+  if (c->profiling) CK(cudaEventRecord(c->pev[0], c->stream));
   CK(gw::launch_stage(c->d, p, c->stream));
-  CK(cudaMemcpyAsync(c->h_out, c->d.out, 16 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  c->launches++;
+  if (c->profiling) CK(cudaEventRecord(c->pev[1], c->stream));
+  CK(cudaMemcpyAsync(c->h_out, c->d.out, 32 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if (c->h_out[gw::kOutError] != 0.0) {
+    double z = 0.0;
+    CK(cudaMemcpy(c->d.out + gw::kOutError, &z, sizeof z, cudaMemcpyHostToDevice));
+    return set_err(GW_EINVAL, "FRU stage [%g, %g]: substep limit reached (corrupted FRU state: NaN or "
+                   "out-of-range concentrations)", t0, tf);
+  }
+  if (c->profiling) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->pev[0], c->pev[1]));
+    c->prof_ms += ms;
+    c->prof_launches++;
+  }
   if (num)
     for (int k = 0; k < 5; k++) num[k] = c->h_out[k];
   if (out)
@@ -266,6 +297,7 @@ extern "C" int gw_avg_sums(gw_ctx* c, double num[11]) {
   int rc = flush_pending(c);
   if (rc) return rc;
   CK(gw::launch_avg(c->d, c->stream));
+  c->launches++;
   CK(cudaMemcpyAsync(c->h_out + 16, c->d.out + 16, 11 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < 11; k++) num[k] = c->h_out[16 + k];
@@ -299,5 +331,59 @@ extern "C" int gw_substeps(gw_ctx* c, unsigned long long* count) {
   if (!c || !count) return set_err(GW_EINVAL, "gw_substeps: null argument");
   CK(cudaMemcpyAsync(count, c->d.substeps, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  return GW_OK;
+}
+
+extern "C" int gw_event_record(gw_ctx* c, int slot) {
+  if (!c || slot < 0 || slot > 7) return set_err(GW_EINVAL, "gw_event_record: bad slot");
+  CK(cudaEventRecord(c->ev[slot], c->stream));
+  return GW_OK;
+}
+
+extern "C" int gw_event_elapsed(gw_ctx* c, int a, int b, float* ms) {
+  if (!c || !ms || a < 0 || a > 7 || b < 0 || b > 7) return set_err(GW_EINVAL, "gw_event_elapsed: bad slot");
+  CK(cudaEventSynchronize(c->ev[b]));
+  CK(cudaEventElapsedTime(ms, c->ev[a], c->ev[b]));
+  return GW_OK;
+}
+
+extern "C" int gw_profile(gw_ctx* c, int enable) {
+  if (!c) return set_err(GW_EINVAL, "gw_profile: null context");
+  c->profiling = enable != 0;
+  c->prof_ms = 0.0;
+  c->prof_launches = 0;
+  return GW_OK;
+}
+
+extern "C" int gw_profile_read(gw_ctx* c, double* ms, unsigned long long* launches) {
+  if (!c) return set_err(GW_EINVAL, "gw_profile_read: null context");
+  if (ms) *ms = c->prof_ms;
+  if (launches) *launches = c->prof_launches;
+  return GW_OK;
+}
+
+extern "C" int gw_launches(gw_ctx* c, unsigned long long* count) {
+  if (!c || !count) return set_err(GW_EINVAL, "gw_launches: null argument");
+  *count = c->launches;
+  return GW_OK;
+}
+
+extern "C" int gw_l2_flush(gw_ctx* c) {
+  const size_t bytes = (size_t)512 << 20;
+  if (!c) return set_err(GW_EINVAL, "gw_l2_flush: null context");
+  if (!c->flush_buf) CK(cudaMalloc(&c->flush_buf, bytes));
+  CK(cudaMemsetAsync(c->flush_buf, c->launches & 0xff, bytes, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return GW_OK;
+}
+
+extern "C" int gw_probe_fp64_peak(double* tflops) {
+  if (!tflops) return set_err(GW_EINVAL, "gw_probe_fp64_peak: null argument");
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  double best = 0.0;
+  CK(gw::probe_fp64(sms, &best));
+  *tflops = best;
   return GW_OK;
 }

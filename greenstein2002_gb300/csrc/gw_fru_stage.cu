@@ -114,9 +114,15 @@ __device__ __forceinline__ int pick_dest(const double r[4], const int d[4], int 
   return d[n];
 }
 
+// Upper bound on substeps of one FRU in one stage.  Valid states need far
+// fewer (dt >= 0.1 / max exit rate, and rates are bounded); corrupted input
+// (NaN or huge concentrations) stops here with an error flag instead of
+// looping without end.
+constexpr uint32_t kMaxSubsteps = 1u << 22;
+
 // One FRU over [t0, tf]: simfru_local.c:83-277.
 __device__ __forceinline__ void advance_fru(const StageParams& p, double y[5], uint32_t w[kClefts], MtRef& rng,
-                                            uint32_t& nsub) {
+                                            uint32_t& nsub, bool& overflow) {
   double dep[3], lopen[kClefts], R0[32];
   int nopen[kClefts];
 #pragma unroll
@@ -129,6 +135,10 @@ __device__ __forceinline__ void advance_fru(const StageParams& p, double y[5], u
   const double interval = p.tf - p.t0;
   double t = p.t0;
   while (t < p.tf) {
+    if (nsub >= kMaxSubsteps) {
+      overflow = true;
+      break;
+    }
     // ---- exit rates at the substep start (fru_rates_local.c:126-777) ----
     const LccBasis lb = lcc_basis(dep[0]);
     const double nu = 1.0;
@@ -232,6 +242,7 @@ __global__ void __launch_bounds__(kStageThreads) fru_stage_kernel(DevState s, St
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   uint32_t nsub = 0;
+  bool overflow = false;
   if (f < s.nfru) {
     const size_t nf = (size_t)s.stride;
     double y[5];
@@ -268,7 +279,8 @@ __global__ void __launch_bounds__(kStageThreads) fru_stage_kernel(DevState s, St
       s.mti_s[f] = mti;
     }
     rng.mti = mti;
-    if (p.flags & kFlagAdvance) advance_fru(p, y, w, rng, nsub);
+    if (p.flags & kFlagAdvance) advance_fru(p, y, w, rng, nsub, overflow);
+    if (overflow) s.out[kOutError] = 1.0;
 #pragma unroll
     for (int i = 0; i < 5; i++) s.frus[i * nf + f] = y[i];
 #pragma unroll

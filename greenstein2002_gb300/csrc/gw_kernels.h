@@ -5,7 +5,12 @@
 
 namespace gw {
 
-constexpr int kStageThreads = 128;
+// One warp per block: a 12,500-FRU cell is 391 warps, fewer than the 608
+// SM sub-partitions of a GB300, so single-warp blocks spread them over all
+// 152 SMs instead of leaving SMs idle.
+constexpr int kStageThreads = 32;
+// out[] slot of the device error flag (substep limit hit)
+constexpr int kOutError = 31;
 
 enum : int {
   kFlagAdvance = 1,  // run the substep loop over [t0, tf]
@@ -21,7 +26,8 @@ enum : int { kSeedBase = 0, kSeedReference = 1 };
 //   *_s               snapshot taken at the last save
 //   mt_hold/hold_epoch  copy-on-twist protection of the saved MT words
 //   partials[nblocks][16], ticket: scratch of the deterministic grid reduction
-//   out[32]           [0..4] flux sums, [5..8] Jxfer,Jtr,ICa,Ito2, [16..26] averages
+//   out[32]           [0..4] flux sums, [5..8] Jxfer,Jtr,ICa,Ito2, [16..26] averages,
+//                     [31] error flag
 struct DevState {
   int nfru, stride, nblocks;
   double* frus;
@@ -49,6 +55,8 @@ struct StageParams {
 
 cudaError_t launch_stage(const DevState& s, const StageParams& p, cudaStream_t st);
 cudaError_t launch_avg(const DevState& s, cudaStream_t st);
+// FP64 FMA throughput of the device (TFLOP/s, best of a few launches).
+cudaError_t probe_fp64(int sms, double* tflops);
 cudaError_t launch_seed(const DevState& s, int scheme, uint32_t base, cudaStream_t st);
 
 }  // namespace gw

@@ -1,0 +1,417 @@
+/*
+ * gw_caf -- C host driver of the GB300 FRU path: the reference program's main
+ * loop (caf.c:43-285) on top of libgw_fru.so, with the run settings of
+ * parameters.h read at run time instead of compiled in.
+ *
+ *   gw_caf [settings-file] [key=value ...]
+ *
+ * Settings file: one `key = value` per line, '#' starts a comment; keys are
+ * the reference's parameters.h macro names (NFRU_sim, time_end, period,
+ * vclamp_flag, ic_file_flag, ic_dir, output_dir, Ndump, ...) plus
+ * seed_scheme (0: seed base+j, 1: initialize_ran.c formula) and seed_base.
+ * Command-line key=value pairs override the file.
+ *
+ * Inputs and outputs keep the reference's formats byte for byte:
+ * ic/stable/ic_*.txt (initialize_state.c:43-163, rewound every
+ * min(NFRU,1250) FRUs), states.N.txt / otherstates.N.txt / currents.N.txt
+ * (data_io.c:22-140), and the r_*.N.txt checkpoint files (data_io.c:197-268)
+ * every Ndump output steps.
+ */
+#include <ctype.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "gw_cell_model.h"
+#include "gw_fru.h"
+
+typedef struct {
+    gw_settings s;
+    int nfru, ts_sec, ic_file_flag, Ndump, filenumber0, seed_scheme;
+    unsigned long seed_base;
+    char ic_dir[512], output_dir[512];
+    char ic_states[128], ic_FRU[128], ic_LCh[128], ic_RyR[128], ic_Ito2[128];
+} run_cfg;
+
+static void cfg_defaults(run_cfg *c)
+{
+    memset(c, 0, sizeof *c);
+    gw_settings_init(&c->s);
+    c->nfru = 1000;            /* parameters.h:43-51 */
+    c->ts_sec = 1;             /* parameters.h:101 */
+    c->ic_file_flag = 1;       /* parameters.h:188 */
+    c->Ndump = 10000;          /* parameters.h:209 */
+    c->filenumber0 = 0;
+    c->seed_scheme = 1;        /* the reference's initialize_ran.c formula */
+    c->seed_base = 5489;
+    strcpy(c->ic_dir, "ic/stable");
+    strcpy(c->output_dir, "./");
+    strcpy(c->ic_states, "ic_states_stable.txt");
+    strcpy(c->ic_FRU, "ic_FRU_stable.txt");
+    strcpy(c->ic_LCh, "ic_LCh_stable.txt");
+    strcpy(c->ic_RyR, "ic_RyR_stable.txt");
+    strcpy(c->ic_Ito2, "ic_Ito2_stable.txt");
+}
+
+static char *trim(char *p)
+{
+    char *e;
+    while (isspace((unsigned char)*p)) p++;
+    e = p + strlen(p);
+    while (e > p && isspace((unsigned char)e[-1])) *--e = 0;
+    if (*p == '"' && e > p + 1 && e[-1] == '"') {
+        e[-1] = 0;
+        p++;
+    }
+    return p;
+}
+
+static int set_key(run_cfg *c, const char *k, const char *v)
+{
+#define DBL(name) if (!strcmp(k, #name)) { c->s.name = atof(v); return 0; }
+#define INT(name) if (!strcmp(k, #name)) { c->s.name = atoi(v); return 0; }
+    DBL(time_start) DBL(time_end) DBL(time_step) DBL(step_min) DBL(step_max) DBL(tolrk)
+    DBL(pulse_duration) DBL(pulse_amplitude) DBL(period) DBL(shift)
+    INT(vclamp_flag) DBL(vclamp_duration) DBL(vclamp_set) DBL(vclamp_shift) DBL(vclamp_hold) DBL(vclamp_period)
+    INT(vppclamp_flag) DBL(vppclamp_ppset) DBL(vppclamp_ppduration) DBL(vppclamp_shift) DBL(vppclamp_set)
+    DBL(vppclamp_duration) DBL(vppclamp_hold) DBL(vppclamp_period)
+    INT(iv_flag) DBL(iv_clamp_duration) DBL(iv_clamp_period) DBL(iv_shift) DBL(iv_clamp_set) DBL(iv_clamp_hold)
+    DBL(iv_clamp_step)
+    INT(chf_flag) DBL(chfsc_IK1) DBL(chfsc_Jup) DBL(chfsc_INaCa) DBL(chfsc_IKv43) DBL(scale_PCa) DBL(scale_GKr)
+#undef DBL
+#undef INT
+    if (!strcmp(k, "NFRU_sim") || !strcmp(k, "NFRU_sim_high") || !strcmp(k, "NFRU")) { c->nfru = atoi(v); return 0; }
+    if (!strcmp(k, "ts_sec")) { c->ts_sec = atoi(v); return 0; }
+    if (!strcmp(k, "ic_file_flag")) { c->ic_file_flag = atoi(v); return 0; }
+    if (!strcmp(k, "Ndump")) { c->Ndump = atoi(v); return 0; }
+    if (!strcmp(k, "filenumber0")) { c->filenumber0 = atoi(v); return 0; }
+    if (!strcmp(k, "seed_scheme")) { c->seed_scheme = atoi(v); return 0; }
+    if (!strcmp(k, "seed_base")) { c->seed_base = strtoul(v, NULL, 10); return 0; }
+#define STR(field, name) if (!strcmp(k, name)) { snprintf(c->field, sizeof c->field, "%s", v); return 0; }
+    STR(ic_dir, "ic_dir") STR(output_dir, "output_dir") STR(ic_states, "ic_states_file") STR(ic_FRU, "ic_FRU_file")
+    STR(ic_LCh, "ic_LCh_file") STR(ic_RyR, "ic_RyR_file") STR(ic_Ito2, "ic_Ito2_file")
+#undef STR
+    return -1;
+}
+
+static int parse_line(run_cfg *c, char *line, const char *where)
+{
+    char *h = strchr(line, '#'), *eq, *k, *v;
+    if (h) *h = 0;
+    k = trim(line);
+    if (!*k) return 0;
+    eq = strchr(k, '=');
+    if (!eq) {
+        fprintf(stderr, "%s: expected key = value: '%s'\n", where, k);
+        return -1;
+    }
+    *eq = 0;
+    v = trim(eq + 1);
+    k = trim(k);
+    if (set_key(c, k, v)) {
+        fprintf(stderr, "%s: unknown setting '%s'\n", where, k);
+        return -1;
+    }
+    return 0;
+}
+
+/* ---- tolerant readers of the IC files (data_io.c:142-194) ---------------- */
+static double read_next_double(FILE *f)
+{
+    char buf[256];
+    int ch, i = 0;
+    do ch = fgetc(f); while (ch != EOF && isspace(ch));
+    while (ch != EOF && (isdigit(ch) || ch == 'E' || ch == 'e' || ch == '-' || ch == '+' || ch == '.') && i < 255) {
+        buf[i++] = (char)ch;
+        ch = fgetc(f);
+    }
+    buf[i] = 0;
+    if (i < 1) {
+        fprintf(stderr, "Error reading ic file: no decent input!\n");
+        return 0;
+    }
+    return strtod(buf, NULL);
+}
+
+static int read_next_int(FILE *f)
+{
+    char buf[256];
+    int ch, i = 0;
+    do ch = fgetc(f); while (ch != EOF && isspace(ch));
+    while (ch != EOF && (isdigit(ch) || ch == '-' || ch == '+') && i < 255) {
+        buf[i++] = (char)ch;
+        ch = fgetc(f);
+    }
+    buf[i] = 0;
+    if (i < 1 || i > 30) {
+        fprintf(stderr, "Error reading ic file: no decent input!\n");
+        return 0;
+    }
+    return (int)strtol(buf, NULL, 10);
+}
+
+static FILE *open_ic(const run_cfg *c, const char *name)
+{
+    char path[1200];
+    FILE *f;
+    snprintf(path, sizeof path, "%s/%s", c->ic_dir, name);
+    if (!(f = fopen(path, "rb"))) {
+        fprintf(stderr, "Cannot open file '%s'!\n", path);
+        exit(2);
+    }
+    return f;
+}
+
+/* FRU and global initial conditions from ic files (initialize_state.c:43-133),
+ * each file rewound after every min(NFRU,1250) FRUs. */
+static void read_ic(const run_cfg *c, double *state, double *frus, int *ltype, int *ryr, int *ito2)
+{
+    const int n = c->nfru, rw = n < 1250 ? n : 1250;
+    FILE *f;
+    int j, k;
+    f = open_ic(c, c->ic_RyR);
+    read_next_int(f);
+    for (j = 0; j < n; j++) {
+        for (k = 0; k < 20; k++) ryr[20 * j + k] = read_next_int(f);
+        if ((j + 1) % rw == 0) { rewind(f); read_next_int(f); }
+    }
+    fclose(f);
+    f = open_ic(c, c->ic_LCh);
+    read_next_int(f);
+    for (j = 0; j < n; j++) {
+        for (k = 0; k < 8; k++) ltype[8 * j + k] = read_next_int(f);
+        if ((j + 1) % rw == 0) { rewind(f); read_next_int(f); }
+    }
+    fclose(f);
+    f = open_ic(c, c->ic_Ito2);
+    read_next_int(f);
+    for (j = 0; j < n; j++) {
+        for (k = 0; k < 4; k++) ito2[4 * j + k] = read_next_int(f);
+        if ((j + 1) % rw == 0) { rewind(f); read_next_int(f); }
+    }
+    fclose(f);
+    f = open_ic(c, c->ic_FRU);
+    read_next_int(f);
+    for (j = 0; j < n; j++) {
+        for (k = 0; k < 5; k++) frus[5 * j + k] = read_next_double(f);
+        if ((j + 1) % rw == 0) { rewind(f); read_next_int(f); }
+    }
+    fclose(f);
+    f = open_ic(c, c->ic_states);
+    for (k = 0; k < GW_NSTATE; k++) state[k] = read_next_double(f);
+    fclose(f);
+}
+
+/* ---- output files (data_io.c:22-140) ------------------------------------ */
+static FILE *open_out(const run_cfg *c, const char *stem, int num)
+{
+    char path[1200];
+    FILE *f;
+    snprintf(path, sizeof path, "%s%s.%d.txt", c->output_dir, stem, num);
+    if (!(f = fopen(path, "w+"))) {
+        fprintf(stderr, "Cannot open file '%s'!\n", path);
+        exit(3);
+    }
+    return f;
+}
+
+static FILE *open_states(const run_cfg *c, int num)
+{
+    FILE *f = open_out(c, "states", num);
+    fprintf(f, "Time V mNa hNa jNa Nai Ki Cai CaNSR xKs LTRPNCa HTRPNCa C0Kv43 C1Kv43 C2Kv43 C3Kv43 OKv43 CI0Kv43 "
+               "CI1Kv43 CI2Kv43 CI3Kv43 OIKv43 C0Kv14 C1Kv14 C2Kv14 C3Kv14 OKv14 CI0Kv14 CI1Kv14 CI2Kv14 CI3Kv14 "
+               "OIKv14 CaToT C1Herg C2Herg C3Herg OHerg IHerg\n");
+    return f;
+}
+
+static FILE *open_otherstates(const run_cfg *c, int num)
+{
+    FILE *f = open_out(c, "otherstates", num);
+    fprintf(f, "Time CaSSavg CaJSRavg JRyRtot PRyR_open PRyR_ready PNorm_mode PnotVinact PLType_open CaToT2 "
+               "PIto2_open CaJSRtot CaSStot \n");
+    return f;
+}
+
+static FILE *open_currents(const run_cfg *c, int num)
+{
+    FILE *f = open_out(c, "currents", num);
+    fprintf(f, "Time INa IKr IKs Ito1 IK1 IKp INaCa INaK IpCa ICab INab ICa JDHPR Jup Jtrpn Jtr Jxfer IKv43 IKv14 "
+               "IKv14_K IKv14_Na Ito2 Istim Itot \n");
+    return f;
+}
+
+static void write_row(FILE *f, const run_cfg *c, double t, const double *v, int n, const char *fmt)
+{
+    int i;
+    fprintf(f, "%g ", c->ts_sec ? t * 1.e-3 : t);
+    for (i = 0; i < n; i++) fprintf(f, fmt, v[i]);
+    fprintf(f, "\n");
+}
+
+/* checkpoint files r_*.N.txt (data_io.c:197-268) */
+static void restart_data(const run_cfg *c, int num, const double *state, gw_ctx *ctx)
+{
+    const int n = c->nfru;
+    double *frus = malloc(sizeof(double) * 5 * n);
+    int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n), *ito2 = malloc(sizeof(int) * 4 * n);
+    FILE *fs, *ff, *fl, *fr, *fi;
+    int j, k, q;
+    if (!frus || !ltype || !ryr || !ito2 || gw_download(ctx, frus, ltype, ryr, ito2, NULL, NULL)) {
+        fprintf(stderr, "restart_data: download failed: %s\n", gw_last_error());
+        exit(4);
+    }
+    fs = open_out(c, "r_states", num);
+    for (k = 0; k < GW_NSTATE; k++) fprintf(fs, "%g\n", state[k]);
+    ff = open_out(c, "r_FRU", num);
+    fl = open_out(c, "r_LCh", num);
+    fr = open_out(c, "r_RyR", num);
+    fi = open_out(c, "r_Ito2", num);
+    fprintf(ff, "%d\n", n);
+    fprintf(fr, "%d\n", n);
+    fprintf(fl, "%d\n", n);
+    fprintf(fi, "%d\n", n);
+    for (j = 0; j < n; j++) {
+        for (k = 0; k < 5; k++) fprintf(ff, "%g ", frus[5 * j + k]);
+        fprintf(ff, "\n");
+        for (q = 0; q < 4; q++) {
+            fprintf(fl, "%d %d\n", ltype[8 * j + 2 * q], ltype[8 * j + 2 * q + 1]);
+            for (k = 0; k < 5; k++) fprintf(fr, "%d ", ryr[20 * j + 5 * q + k]);
+            fprintf(fr, "\n");
+            fprintf(fi, "%d\n", ito2[4 * j + q]);
+        }
+    }
+    fclose(ff); fclose(fs); fclose(fr); fclose(fl); fclose(fi);
+    free(frus); free(ltype); free(ryr); free(ito2);
+}
+
+/* initial conditions (initialize_ran.c + initialize_state.c) */
+static void init_cell(const run_cfg *c, gw_ctx *ctx, double *state)
+{
+    const int n = c->nfru;
+    if (!c->ic_file_flag) {
+        if (gw_init_rest(ctx, &c->s, c->seed_scheme, (uint32_t)c->seed_base, state)) {
+            fprintf(stderr, "gw_init_rest: %s\n", gw_last_error());
+            exit(5);
+        }
+        return;
+    }
+    {
+        double *frus = malloc(sizeof(double) * 5 * n), a1 = 0.0, a2 = 0.0;
+        int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n);
+        int *ito2 = malloc(sizeof(int) * 4 * n), *mti = malloc(sizeof(int) * n), j, q;
+        uint32_t *mt = calloc((size_t)624 * n, sizeof(uint32_t));
+        read_ic(c, state, frus, ltype, ryr, ito2);
+        for (j = 0; j < n; j++) mti[j] = 624;
+        if (gw_upload(ctx, frus, ltype, ryr, ito2, mti, mt) || gw_seed(ctx, c->seed_scheme, (uint32_t)c->seed_base)) {
+            fprintf(stderr, "initial upload failed: %s\n", gw_last_error());
+            exit(5);
+        }
+        if (c->s.vclamp_flag) state[GW_V] = c->s.vclamp_hold;
+        if (c->s.iv_flag) state[GW_V] = c->s.iv_clamp_hold;
+        for (j = 0; j < n; j++) {
+            a1 = a1 + frus[5 * j] * (1.0 + GWC_CSQNtot / (GWC_KmCSQN + frus[5 * j]));
+            for (q = 0; q < 4; q++)
+                a2 = a2 + frus[5 * j + q + 1] * (1.0 + GWC_BSRtot / (GWC_KBSR + frus[5 * j + q + 1]) +
+                                                  GWC_BSLtot / (GWC_KBSL + frus[5 * j + q + 1]));
+        }
+        state[GW_CaTOT] = gw_catot(a1, a2, 12500.0 / n, state);
+        if (c->s.vclamp_flag) state[GW_V] = c->s.vclamp_hold;
+        free(frus); free(ltype); free(ryr); free(ito2); free(mti); free(mt);
+    }
+}
+
+int main(int argc, char **argv)
+{
+    run_cfg c;
+    gw_ctx *ctx = NULL;
+    double state[GW_NSTATE], cur[GW_NCUR], other[GW_NOTHER], num[11];
+    double time_now, tstep, oldstep, iv_time = 0.0;
+    int filenumber, n_restart = 0, a, rc;
+    FILE *fst, *fcu, *fot;
+    clock_t c0 = clock();
+
+    cfg_defaults(&c);
+    for (a = 1; a < argc; a++) {
+        if (strchr(argv[a], '=')) {
+            char buf[1024];
+            snprintf(buf, sizeof buf, "%s", argv[a]);
+            if (parse_line(&c, buf, "command line")) return 1;
+        } else {
+            FILE *f = fopen(argv[a], "r");
+            char line[1024];
+            if (!f) {
+                fprintf(stderr, "Cannot open settings file '%s'\n", argv[a]);
+                return 1;
+            }
+            while (fgets(line, sizeof line, f))
+                if (parse_line(&c, line, argv[a])) return 1;
+            fclose(f);
+        }
+    }
+    if ((rc = gw_create(&ctx, c.nfru))) {
+        fprintf(stderr, "gw_create: %s\n", gw_last_error());
+        return 1;
+    }
+    gw_set_scale(ctx, 12500.0 / c.nfru);
+    oldstep = c.s.step_max;
+    filenumber = c.filenumber0;
+    init_cell(&c, ctx, state);
+    fst = open_states(&c, filenumber);
+    fcu = open_currents(&c, filenumber);
+    fot = open_otherstates(&c, filenumber);
+    printf("%s %s %s %s\n", "Time", "Phase", "NFRU", "V");
+    for (time_now = c.s.time_start; time_now <= c.s.time_end - .0001 * c.s.time_step; time_now += c.s.time_step) {
+        printf("%g %i %i %g\n", time_now, 1, c.nfru, state[GW_V]);
+        n_restart = n_restart + 1;
+        tstep = time_now + c.s.time_step;
+        iv_time = iv_time + c.s.time_step;
+        if ((rc = gw_rk54pd(ctx, &c.s, time_now, tstep, oldstep, state, cur, &oldstep)) ||
+            (rc = gw_avg_sums(ctx, num))) {
+            fprintf(stderr, "step at t=%g failed: %s\n", time_now, gw_last_error());
+            return 1;
+        }
+        gw_otherstates(num, c.nfru, 12500.0 / c.nfru, state, other);
+        if (time_now > c.s.time_start) {
+            if (n_restart == 1) {
+                fclose(fcu);
+                fcu = open_currents(&c, filenumber);
+            } else {
+                write_row(fcu, &c, time_now, cur, GW_NCUR, "%g ");
+            }
+        }
+        write_row(fst, &c, tstep, state, GW_NSTATE, "%.8g ");
+        write_row(fot, &c, tstep, other, GW_NOTHER, "%g ");
+        if (n_restart >= c.Ndump) {
+            n_restart = 0;
+            restart_data(&c, filenumber, state, ctx);
+            filenumber = filenumber + 1;
+            fclose(fot);
+            fclose(fst);
+            if (time_now < c.s.time_end - 1.0001 * c.s.time_step) {
+                fst = open_states(&c, filenumber);
+                fot = open_otherstates(&c, filenumber);
+            } else {
+                fst = fot = NULL;
+            }
+        }
+        if (c.s.iv_flag && iv_time >= c.s.iv_clamp_period) {
+            iv_time = 0.0;
+            c.s.iv_n = c.s.iv_n + 1;
+            oldstep = c.s.step_max;
+            init_cell(&c, ctx, state);
+        }
+    }
+    if ((rc = gw_lastcall(ctx, &c.s, c.s.time_end, state, cur))) {
+        fprintf(stderr, "lastcall failed: %s\n", gw_last_error());
+        return 1;
+    }
+    write_row(fcu, &c, c.s.time_end, cur, GW_NCUR, "%g ");
+    fclose(fcu);
+    if (fot) fclose(fot);
+    if (fst) fclose(fst);
+    gw_destroy(ctx);
+    printf("Total time: %fs\n", (double)(clock() - c0) / (double)CLOCKS_PER_SEC);
+    return 0;
+}

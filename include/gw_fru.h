@@ -84,6 +84,18 @@ int gw_substeps(gw_ctx *ctx, unsigned long long *count);
 /* Wait for all work of the context. */
 int gw_sync(gw_ctx *ctx);
 
+/* Measurement helpers on the context's stream (no reference counterpart):
+ * events in slots 0..7; per-launch device time of the FRU stage kernel while
+ * profiling is enabled; kernel-launch counter; an L2 flush (writes 512 MB);
+ * a measured FP64 FMA peak of the device in TFLOP/s. */
+int gw_event_record(gw_ctx *ctx, int slot);
+int gw_event_elapsed(gw_ctx *ctx, int slot_a, int slot_b, float *ms);
+int gw_profile(gw_ctx *ctx, int enable);
+int gw_profile_read(gw_ctx *ctx, double *stage_kernel_ms, unsigned long long *stage_launches);
+int gw_launches(gw_ctx *ctx, unsigned long long *count);
+int gw_l2_flush(gw_ctx *ctx);
+int gw_probe_fp64_peak(double *tflops);
+
 /* Run settings of parameters.h:92-156 as a runtime struct; see
  * gw_protocol_init for the defaults (the reference's parameters.h values). */
 typedef struct gw_settings {

@@ -45,7 +45,7 @@ LIB_SOURCES = [
     "initialize_ran.c", "mpi_master.c", "mpi_slave.c", "rk_pd54m.c",
 ]
 WRAPS = ["initialize_ran", "initialize_mpi_state", "distrib_simFRU", "send_calc_fru_flux",
-         "send_calc_fru_avg", "send_save_state", "send_resume_state", "end_mpi"]
+         "send_calc_fru_avg", "send_save_state", "send_resume_state", "end_mpi", "fcn"]
 CFLAGS = ["-O3", "-ffp-contract=off", "-fno-strict-aliasing", "-w"]
 
 

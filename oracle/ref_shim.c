@@ -8,7 +8,8 @@
  *  GW_SHIM_EXE  -- linked into the serial reference executable with
  *                  -Wl,--wrap=<fn> for the FRU-layer entry points that
  *                  caf.c / rk_pd54m.c / fcn.c call (mpi_master.c:41,122,199,
- *                  369,477,493,643; initialize_ran.c:23).  The wrappers log
+ *                  369,477,493,643; initialize_ran.c:23; fcn.c:29 when it
+ *                  stores currents).  The wrappers log
  *                  every call (inputs and outputs) to the binary file named
  *                  by $GW_REF_LOG and dump the initial / final FRU working set
  *                  (the *_local globals of mpi_slave.c:31-45) to
@@ -135,6 +136,20 @@ void __real_send_save_state(void);
 void __wrap_send_save_state(void) { log_rec('V', NULL, 0); __real_send_save_state(); }
 void __real_send_resume_state(void);
 void __wrap_send_resume_state(void) { log_rec('R', NULL, 0); __real_send_resume_state(); }
+
+void __real_fcn(const double, double[N], double[N], double[Ncur], const int, const double, const double,
+                const double, const double);
+void __wrap_fcn(const double t, double state[N], double F[N], double cur[Ncur], const int keepc, const double Jxfer,
+                const double Jtr, const double ICa, const double Ito2)
+{
+    __real_fcn(t, state, F, cur, keepc, Jxfer, Jtr, ICa, Ito2);
+    if (keepc) {
+        double rec[1 + Ncur];
+        rec[0] = t;
+        memcpy(rec + 1, cur, Ncur * sizeof(double));
+        log_rec('C', rec, 1 + Ncur);
+    }
+}
 
 void __real_end_mpi(void);
 void __wrap_end_mpi(void)

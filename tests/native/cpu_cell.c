@@ -44,14 +44,15 @@ static void free_set(set_t *s)
 {
     free(s->frus); free(s->ltype); free(s->ryr); free(s->ito2); free(s->mti); free(s->mt);
 }
+/* NULL destination arrays are skipped (gw_download's optional outputs) */
 static void copy_set(set_t *d, const set_t *s, int n)
 {
-    memcpy(d->frus, s->frus, sizeof(double) * 5 * n);
-    memcpy(d->ltype, s->ltype, sizeof(int) * 8 * n);
-    memcpy(d->ryr, s->ryr, sizeof(int) * 20 * n);
-    memcpy(d->ito2, s->ito2, sizeof(int) * 4 * n);
-    memcpy(d->mti, s->mti, sizeof(int) * n);
-    memcpy(d->mt, s->mt, sizeof(uint32_t) * 624 * n);
+    if (d->frus) memcpy(d->frus, s->frus, sizeof(double) * 5 * n);
+    if (d->ltype) memcpy(d->ltype, s->ltype, sizeof(int) * 8 * n);
+    if (d->ryr) memcpy(d->ryr, s->ryr, sizeof(int) * 20 * n);
+    if (d->ito2) memcpy(d->ito2, s->ito2, sizeof(int) * 4 * n);
+    if (d->mti) memcpy(d->mti, s->mti, sizeof(int) * n);
+    if (d->mt) memcpy(d->mt, s->mt, sizeof(uint32_t) * 624 * n);
 }
 
 const char *gw_last_error(void) { return "cpu test stand-in"; }

@@ -1,0 +1,173 @@
+"""Parity of the CUDA FRU path (through the C-ABI) with the CPU oracle and
+with fixtures generated from the reference.
+
+Bar: bit-exact for every integer/index quantity (channel states, MT19937
+words and positions, open counts); FP64 Ca concentrations and flux sums
+within a relative 1e-12 (CUDA's exp() and the host libm's may differ in the
+last unit in the last place; flux sums are summed in a fixed tree order
+instead of the reference's sequential order)."""
+import ctypes as C
+import zlib
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+
+def _mtcrc(mt):
+    return np.array([zlib.crc32(r.tobytes()) for r in mt], np.uint32)
+
+
+def _same_ints(a, b, msg=""):
+    for k in ("ltype", "ryr", "ito2", "mti", "mt"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg="%s %s" % (msg, k))
+
+
+def _random_set(rng, n, base):
+    s = O.rest_set(n, "base", base)
+    s["ltype"][:, :, 0] = rng.integers(1, 13, (n, 4))
+    s["ltype"][:, :, 1] = rng.integers(1, 3, (n, 4))
+    s["ryr"][:] = rng.integers(1, 9, (n, 4, 5))
+    s["ito2"][:] = rng.integers(1, 3, (n, 4))
+    s["frus"][:, 0] = rng.uniform(0.05, 1.2, n)
+    s["frus"][:, 1:] = 10 ** rng.uniform(-4.5, -0.5, (n, 4))
+    s["mti"][:] = rng.integers(0, 625, n)
+    return s
+
+
+def test_device_seeding_matches_oracle(gw):
+    for scheme, name in ((gw.SEED_BASE, "base"), (gw.SEED_REFERENCE, "reference")):
+        n = 1500
+        cell = gw.Cell(n)
+        cell.upload(O.rest_set(n))
+        cell.seed(scheme, 5489)
+        got = cell.download()
+        want = O.rest_set(n, name, 5489)
+        np.testing.assert_array_equal(got["mt"], want["mt"])
+        np.testing.assert_array_equal(got["mti"], want["mti"])
+
+
+def test_upload_download_roundtrip(gw):
+    rng = np.random.default_rng(1)
+    s = _random_set(rng, 777, 11)
+    cell = gw.Cell(777)
+    cell.upload(s)
+    got = cell.download()
+    _same_ints(got, s)
+    np.testing.assert_array_equal(got["frus"], s["frus"])
+
+
+def test_stage_cases_match_reference_fixture(gw):
+    from test_oracle import _case_inputs
+    g = golden("stage_cases.npz")
+    for ci in range(int(g["ncases"][0])):
+        s = _case_inputs(g, ci)
+        cell = gw.Cell(s["frus"].shape[0])
+        cell.upload(s)
+        t0, tf = g["c%d_t" % ci]
+        d0, df = g["c%d_dep" % ci]
+        _, num = cell.stage(t0, tf, d0, df)
+        out = cell.download()
+        for k in ("ltype", "ryr", "ito2", "mti"):
+            np.testing.assert_array_equal(out[k], g["c%d_out_%s" % (ci, k)], err_msg="case %d %s" % (ci, k))
+        np.testing.assert_array_equal(_mtcrc(out["mt"]), g["c%d_out_mtcrc" % ci])
+        np.testing.assert_allclose(out["frus"], g["c%d_out_frus" % ci], rtol=RTOL, atol=0)
+        np.testing.assert_allclose(num, g["c%d_out_flux" % ci], rtol=RTOL, atol=0)
+        np.testing.assert_allclose(cell.avg_sums(), g["c%d_out_avg" % ci], rtol=RTOL, atol=1e-300)
+
+
+@pytest.mark.parametrize("n", [1, 31, 129, 3001])
+def test_random_stages_match_oracle(gw, n):
+    rng = np.random.default_rng(n)
+    s = _random_set(rng, n, 100 + n)
+    cell = gw.Cell(n)
+    cell.upload(s)
+    for k in range(6):
+        v0 = rng.uniform(-100, 60)
+        d0 = np.array([v0, rng.uniform(5e-5, 1e-3), rng.uniform(0.1, 1.2)])
+        df = d0 + np.array([rng.uniform(-8, 8), rng.uniform(-1e-5, 1e-5), rng.uniform(-0.01, 0.01)])
+        t0 = 10.0 * k + rng.uniform(0, 1)
+        tf = t0 + 10 ** rng.uniform(-4, -1)
+        cur, num = cell.stage(t0, tf, d0, df)
+        O.simfru(s, t0, tf, d0, df)
+        want_num = O.flux_sums(s)
+        np.testing.assert_allclose(num, want_num, rtol=RTOL)
+        np.testing.assert_allclose(cur, O.currents(n, 12500.0 / n, df, want_num), rtol=1e-11)
+    got = cell.download()
+    _same_ints(got, s, "n=%d" % n)
+    np.testing.assert_allclose(got["frus"], s["frus"], rtol=RTOL)
+
+
+def test_zero_length_stage_and_flux(gw):
+    rng = np.random.default_rng(5)
+    s = _random_set(rng, 200, 9)
+    cell = gw.Cell(200)
+    cell.upload(s)
+    dep = np.array([-85.0, 1e-4, 0.5])
+    cur, num = cell.flux(dep)
+    np.testing.assert_allclose(num, O.flux_sums(s), rtol=RTOL)
+    cell.stage(3.0, 3.0, dep, dep)
+    got = cell.download()
+    _same_ints(got, s)
+    np.testing.assert_array_equal(got["frus"], s["frus"])
+
+
+def test_save_resume_restores_fru_and_rng_state(gw):
+    """send_save_state / send_resume_state (mpi_slave.c:150-226): a rejected
+    step rolls FRUs and MT streams back, across MT regenerations."""
+    n = 300
+    rng = np.random.default_rng(3)
+    s = _random_set(rng, n, 77)
+    cell = gw.Cell(n)
+    cell.upload(s)
+    d0 = np.array([-20.0, 3e-4, 0.9])
+    df = np.array([-10.0, 3.2e-4, 0.88])
+    cell.save()
+    cell.stage(0.0, 0.5, d0, df)       # ~50-5000 substeps per FRU: many regenerations
+    cell.stage(0.5, 0.9, df, d0)
+    cell.resume()
+    got = cell.download()
+    _same_ints(got, s)
+    np.testing.assert_array_equal(got["frus"], s["frus"])
+    # the retried attempt reproduces the first one exactly
+    a, _ = cell.stage(0.0, 0.5, d0, df)
+    first = cell.download()
+    cell.resume()
+    b, _ = cell.stage(0.0, 0.5, d0, df)
+    second = cell.download()
+    np.testing.assert_array_equal(a, b)
+    _same_ints(first, second)
+    np.testing.assert_array_equal(first["frus"], second["frus"])
+
+
+def test_closed_loop_matches_reference_20ms(gw):
+    """The reference program at NFRU=250 (rest state, 1 Hz, seeds 5489+j):
+    the GPU run reproduces its per-ms global states over the AP upstroke."""
+    g = golden("closed250.npz")
+    cell = gw.Cell(250)
+    st = gw.settings()
+    state = cell.init_rest(st, scheme=gw.SEED_BASE, base=5489)
+    _, states, other, cur = cell.run(state, 0.0, 20, set_=st)
+    np.testing.assert_allclose(states, g["states"], rtol=1e-9, atol=1e-15)
+    np.testing.assert_allclose(other, g["other"], rtol=1e-9, atol=1e-15)
+    fin = cell.download()
+    assert np.mean(fin["mti"] == g["final_mti"]) >= 0.99
+    assert np.mean(np.all(fin["ryr"].reshape(250, -1) == g["final_ryr"].reshape(250, -1), axis=1)) >= 0.99
+
+
+def test_gpu_runs_are_deterministic(gw):
+    outs = []
+    for _ in range(2):
+        cell = gw.Cell(500)
+        st = gw.settings()
+        state = cell.init_rest(st, scheme=gw.SEED_BASE, base=1234)
+        _, states, other, _ = cell.run(state, 5.0, 8, set_=st)
+        outs.append((states, other, cell.download()))
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
+    _same_ints(outs[0][2], outs[1][2])

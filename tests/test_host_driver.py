@@ -1,0 +1,107 @@
+"""The C host driver (greenstein2002_gb300/host/gw_caf.c): run settings at run
+time, the reference's initial-condition readers and output writers.
+
+On CPU the driver is linked against the test-only CPU stand-in of the FRU
+API (tests/native/cpu_cell.c over the oracle); since that composition is bit-
+exact with the reference, its output files must equal the reference
+program's byte for byte -- which pins the file formats (data_io.c:22-140,
+initialize_state.c:43-163) and the main-loop cadence (caf.c:150-255)."""
+import filecmp
+import os
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT, TBUILD, cpu_cell_lib_path
+
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import build_ref  # noqa: E402
+
+
+def cpu_driver():
+    out = os.path.join(TBUILD, "gw_caf_cpu")
+    srcs = [os.path.join(ROOT, "greenstein2002_gb300", "host", "gw_caf.c"),
+            os.path.join(ROOT, "tests", "native", "cpu_cell.c"),
+            os.path.join(ROOT, "greenstein2002_gb300", "csrc", "gw_dp.c"),
+            os.path.join(ROOT, "oracle", "fru_oracle.c")]
+    deps = srcs + [os.path.join(ROOT, "greenstein2002_gb300", "csrc", "gw_cell_model.h"),
+                   os.path.join(ROOT, "include", "gw_fru.h")]
+    if not (os.path.isfile(out) and all(os.path.getmtime(s) <= os.path.getmtime(out) for s in deps)):
+        os.makedirs(TBUILD, exist_ok=True)
+        subprocess.check_call(["gcc", "-O2", "-std=c99", "-ffp-contract=off",
+                               "-I" + os.path.join(ROOT, "greenstein2002_gb300", "csrc"),
+                               "-I" + os.path.join(ROOT, "include"), "-o", out] + srcs + ["-lm"])
+    return out
+
+
+@pytest.fixture(scope="module")
+def have_ref():
+    if not build_ref.have_sources():
+        pytest.skip("reference sources not available")
+
+
+def _run_both(tmp_path, macros, settings, seed_base):
+    d = build_ref.build_config("drv_%d_%d_%d" % (macros["NFRU_sim_high"], int(float(macros["time_end"])),
+                                                 macros["ic_file_flag"]), macros)
+    ref_dir = tmp_path / "ref"
+    build_ref.run_stoch(d, str(ref_dir), seed_base=seed_base)
+    gw_dir = tmp_path / "gw"
+    gw_dir.mkdir()
+    subprocess.run([cpu_driver()] + ["%s=%s" % kv for kv in settings.items()], cwd=gw_dir, check=True,
+                   capture_output=True)
+    return ref_dir, gw_dir
+
+
+def test_outputs_match_reference_rest_start(tmp_path, have_ref):
+    m = build_ref.cfg_macros(250, 15.0)
+    ref_dir, gw_dir = _run_both(tmp_path, m, {"NFRU_sim": 250, "time_end": 15.0, "ic_file_flag": 0,
+                                              "seed_scheme": 0, "seed_base": 5489}, 5489)
+    for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
+        assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
+
+
+def test_outputs_match_reference_ic_files(tmp_path, have_ref):
+    # the reference's default initial conditions: ic/stable files, its own
+    # per-FRU seed formula, 1000 FRUs (1250-FRU files)
+    m = build_ref.cfg_macros(1000, 12.0, ic_file=True)
+    ic = os.path.join(build_ref.SRC, "ic", "stable")
+    ref_dir, gw_dir = _run_both(tmp_path, m, {"NFRU_sim": 1000, "time_end": 12.0, "ic_file_flag": 1,
+                                              "ic_dir": ic, "seed_scheme": 1}, None)
+    for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
+        assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
+
+
+def test_checkpoint_files(tmp_path, have_ref):
+    """r_*.N.txt checkpoints every Ndump steps (data_io.c:197-268).  The
+    reference's restart_data closes the r_states file twice (data_io.c:220
+    and :265), which glibc aborts on, so its process dies after writing
+    r_states and r_FRU; those two are compared byte for byte, the other three
+    (never flushed by the reference) are checked for format and content."""
+    import numpy as np
+    m = build_ref.cfg_macros(64, 7.0)
+    m["Ndump"] = 3
+    d = build_ref.build_config("drv_ckpt", m)
+    ref_dir = tmp_path / "ref"
+    with pytest.raises(RuntimeError, match="double free"):
+        build_ref.run_stoch(d, str(ref_dir), seed_base=77)
+    gw_dir = tmp_path / "gw"
+    gw_dir.mkdir()
+    subprocess.run([cpu_driver(), "NFRU_sim=64", "time_end=7", "ic_file_flag=0", "Ndump=3", "seed_scheme=0",
+                    "seed_base=77"], cwd=gw_dir, check=True, capture_output=True)
+    for f in ("r_states.0.txt", "r_FRU.0.txt"):
+        assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
+    for name, per_line, lo, hi in (("r_LCh", 2, 1, 12), ("r_RyR", 5, 1, 8), ("r_Ito2", 1, 1, 2)):
+        for num in (0, 1):
+            lines = open(gw_dir / ("%s.%d.txt" % (name, num))).read().splitlines()
+            assert int(lines[0]) == 64 and len(lines) == 1 + 64 * 4
+            vals = np.array([[int(x) for x in ln.split()] for ln in lines[1:]])
+            assert vals.shape == (256, per_line) and vals.min() >= lo and vals.max() <= hi
+    assert sorted(os.listdir(gw_dir)) == sorted(
+        ["%s.%d.txt" % (n, k) for n in ("states", "otherstates", "currents") for k in (0, 1, 2)] +
+        ["%s.%d.txt" % (n, k) for n in ("r_states", "r_FRU", "r_LCh", "r_RyR", "r_Ito2") for k in (0, 1)])
+
+
+def test_bad_settings_are_rejected(tmp_path):
+    r = subprocess.run([cpu_driver(), "no_such_key=3"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode != 0 and "unknown setting" in r.stderr
