@@ -25,6 +25,7 @@ CUDA_UNITS = {
     "gw_fru_stage.cu": ["-fmad=false"],
     "gw_abi.cu": [],
     "gw_probe.cu": [],
+    "gw_noalloc.cu": ["-fmad=false"],
 }
 C_UNITS = ["gw_dp.c", "gw_dropin.c"]
 

@@ -53,6 +53,9 @@ struct gw_ctx {
 
 extern "C" const char* gw_last_error(void) { return g_err; }
 
+// error reporting for entry points defined in other translation units
+extern "C" int gw_internal_error(int code, const char* msg) { return set_err(code, "%s", msg); }
+
 extern "C" int gw_nfru(const gw_ctx* c) { return c ? c->d.nfru : 0; }
 
 static void free_dev(gw_ctx* c) {

@@ -96,6 +96,25 @@ int gw_launches(gw_ctx *ctx, unsigned long long *count);
 int gw_l2_flush(gw_ctx *ctx);
 int gw_probe_fp64_peak(double *tflops);
 
+/* Allocation-free FRU stage (no counterpart in the reference).  For callers
+ * that cannot allocate device memory while they run -- cudaMalloc
+ * synchronises the device, is not allowed during stream capture, and is off
+ * limits to hosts that own all device memory -- this advances FRU arrays the
+ * caller owns on the device over [t0, tf] exactly as gw_stage does and writes
+ * out[0..4] = flux sums, out[5..8] = Jxfer, Jtr, ICa, Ito2, out[9] = error
+ * flag (a device or host-mapped array of 10 doubles).  Arrays use the device
+ * layout of gw_stage: frus[5][stride] f64, chan[4][stride] packed channel
+ * words (LCC, VDI, RyR0..4, ClCh nibbles), mti[stride], mt[nfru][640] words.
+ * Its reduction scratch is a fixed array inside the library (about 80 KB per
+ * GPU, held until the process exits), which limits nfru to 65,536; larger
+ * cells get GW_EINVAL.  No save/resume snapshot is taken on this path.  The
+ * first call on a device resolves the scratch address, so make it before any
+ * stream capture.  All calls share the scratch: calls that overlap on the GPU
+ * (different streams, or different cells at once) race and must be
+ * serialised by the caller.  Asynchronous on `stream` (a cudaStream_t). */
+int gw_stage_noalloc(int nfru, int stride, double *frus, uint32_t *chan, int *mti, uint32_t *mt, double t0, double tf,
+                     const double dep0[3], const double depf[3], double nfru_scale, double *out, void *stream);
+
 /* Run settings of parameters.h:92-156 as a runtime struct; see
  * gw_protocol_init for the defaults (the reference's parameters.h values). */
 typedef struct gw_settings {
