@@ -90,6 +90,7 @@ def bind(path):
         "gw_resume": ([vp], C.c_int),
         "gw_substeps": ([vp, P(C.c_ulonglong)], C.c_int),
         "gw_sync": ([vp], C.c_int),
+        "gw_set_fru_lanes": ([vp, C.c_int], C.c_int),
         "gw_settings_init": ([P(Settings)], None),
         "gw_rk54pd": ([vp, P(Settings), C.c_double, C.c_double, C.c_double, _dp, _dp, P(C.c_double)], C.c_int),
         "gw_lastcall": ([vp, P(Settings), C.c_double, _dp, _dp], C.c_int),
@@ -137,13 +138,15 @@ def _ptr(a):
 class Cell:
     """Device-resident FRU state of one cell (a gw_ctx)."""
 
-    def __init__(self, nfru, nfru_scale=None, lib=None):
+    def __init__(self, nfru, nfru_scale=None, lib=None, fru_lanes=None):
         self._L = L = lib if lib is not None else load()
         self._h = C.c_void_p()
         _check(L.gw_create(C.byref(self._h), int(nfru)), "gw_create", self._L)
         self.nfru = int(nfru)
         if nfru_scale is not None:
             _check(L.gw_set_scale(self._h, float(nfru_scale)), "gw_set_scale", self._L)
+        if fru_lanes is not None and hasattr(L, "gw_set_fru_lanes"):
+            _check(L.gw_set_fru_lanes(self._h, int(fru_lanes)), "gw_set_fru_lanes", self._L)
 
     def close(self):
         if self._h:

@@ -23,6 +23,7 @@ NVCC_COMMON = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ff
 CUDA_UNITS = {
     # source: extra flags
     "gw_fru_stage.cu": ["-fmad=false"],
+    "gw_fru_stage4.cu": ["-fmad=false"],
     "gw_abi.cu": [],
     "gw_probe.cu": [],
     "gw_noalloc.cu": ["-fmad=false"],

@@ -49,7 +49,12 @@ struct gw_ctx {
   double prof_ms = 0.0;
   unsigned long long prof_launches = 0, launches = 0;
   void* flush_buf = nullptr;
+  int fru_lanes = 4;        // lanes per FRU of the stage kernel: 1 or 4
 };
+
+static cudaError_t launch_stage_variant(gw_ctx* c, const StageParams& p) {
+  return c->fru_lanes == 4 ? gw::launch_stage4(c->d, p, c->stream) : gw::launch_stage(c->d, p, c->stream);
+}
 
 extern "C" const char* gw_last_error(void) { return g_err; }
 
@@ -97,7 +102,8 @@ extern "C" int gw_create(gw_ctx** out, int nfru) {
   AL(d.mti_s, nf * sizeof(int));
   AL(d.mt_hold, nf * gw::kMtStride * sizeof(uint32_t));
   AL(d.hold_epoch, nf * sizeof(uint32_t));
-  AL(d.partials, (size_t)d.nblocks * 16 * sizeof(double));
+  // partial sums of the widest grid: 8-FRU blocks of the cleft-parallel kernel
+  AL(d.partials, (size_t)((nfru + 7) / 8) * 16 * sizeof(double));
   AL(d.ticket, sizeof(unsigned));
   AL(d.out, 32 * sizeof(double));
   AL(d.substeps, sizeof(unsigned long long));
@@ -136,6 +142,12 @@ extern "C" int gw_destroy(gw_ctx* c) {
 extern "C" int gw_set_scale(gw_ctx* c, double nfru_scale) {
   if (!c) return set_err(GW_EINVAL, "gw_set_scale: null context");
   c->nfru_scale = nfru_scale;
+  return GW_OK;
+}
+
+extern "C" int gw_set_fru_lanes(gw_ctx* c, int lanes) {
+  if (!c || (lanes != 1 && lanes != 4)) return set_err(GW_EINVAL, "gw_set_fru_lanes: lanes must be 1 or 4");
+  c->fru_lanes = lanes;
   return GW_OK;
 }
 
@@ -199,7 +211,7 @@ static int flush_pending(gw_ctx* c) {
   p.epoch = c->epoch;
   p.nfru_scale = c->nfru_scale;
   c->pending = 0;
-  CK(gw::launch_stage(c->d, p, c->stream));
+  CK(launch_stage_variant(c, p));
   c->launches++;
   return GW_OK;
 }
@@ -260,7 +272,7 @@ static int run_stage(gw_ctx* c, double t0, double tf, const double dep0[3], cons
   p.flags = c->pending | (advance ? gw::kFlagAdvance : 0);
   c->pending = 0;
   if (c->profiling) CK(cudaEventRecord(c->pev[0], c->stream));
-  CK(gw::launch_stage(c->d, p, c->stream));
+  CK(launch_stage_variant(c, p));
   c->launches++;
   if (c->profiling) CK(cudaEventRecord(c->pev[1], c->stream));
   CK(cudaMemcpyAsync(c->h_out, c->d.out, 32 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -54,6 +54,8 @@ struct StageParams {
 };
 
 cudaError_t launch_stage(const DevState& s, const StageParams& p, cudaStream_t st);
+// cleft-parallel variant: 4 lanes per FRU, 8 FRUs per single-warp block
+cudaError_t launch_stage4(const DevState& s, const StageParams& p, cudaStream_t st);
 cudaError_t launch_avg(const DevState& s, cudaStream_t st);
 // FP64 FMA throughput of the device (TFLOP/s, best of a few launches).
 cudaError_t probe_fp64(int sms, double* tflops);

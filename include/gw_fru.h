@@ -79,6 +79,11 @@ int gw_avg_sums(gw_ctx *ctx, double num[11]);
 int gw_save(gw_ctx *ctx);
 int gw_resume(gw_ctx *ctx);
 
+/* Lanes per FRU of the FP64 stage kernel: 4 (default) = one lane per cleft,
+ * 8 FRUs per warp, shortest FP64 chain per FRU; 1 = one thread per FRU, 32
+ * FRUs per warp.  Results are identical; the choice only changes speed. */
+int gw_set_fru_lanes(gw_ctx *ctx, int lanes);
+
 /* FRU-substeps executed since creation (workload counter). */
 int gw_substeps(gw_ctx *ctx, unsigned long long *count);
 /* Wait for all work of the context. */

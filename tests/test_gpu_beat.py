@@ -12,9 +12,10 @@ from conftest import golden
 pytestmark = pytest.mark.gpu
 
 
-def test_first_beat_transition_sequences(gw):
+@pytest.mark.parametrize("lanes", [1, 4])
+def test_first_beat_transition_sequences(gw, lanes):
     g = golden("beat250.npz")
-    cell = gw.Cell(250)
+    cell = gw.Cell(250, fru_lanes=lanes)
     st = gw.settings()
     state = cell.init_rest(st, scheme=gw.SEED_BASE, base=5489)
     _, states, other, _ = cell.run(state, 0.0, 1000, set_=st, want=("states", "other"))

@@ -17,6 +17,8 @@ from conftest import golden
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-12
+# stage-kernel variants: 1 = one thread per FRU, 4 = one lane per cleft
+LANES = [1, 4]
 
 
 def _mtcrc(mt):
@@ -52,22 +54,24 @@ def test_device_seeding_matches_oracle(gw):
         np.testing.assert_array_equal(got["mti"], want["mti"])
 
 
-def test_upload_download_roundtrip(gw):
+@pytest.mark.parametrize("lanes", LANES)
+def test_upload_download_roundtrip(gw, lanes):
     rng = np.random.default_rng(1)
     s = _random_set(rng, 777, 11)
-    cell = gw.Cell(777)
+    cell = gw.Cell(777, fru_lanes=lanes)
     cell.upload(s)
     got = cell.download()
     _same_ints(got, s)
     np.testing.assert_array_equal(got["frus"], s["frus"])
 
 
-def test_stage_cases_match_reference_fixture(gw):
+@pytest.mark.parametrize("lanes", LANES)
+def test_stage_cases_match_reference_fixture(gw, lanes):
     from test_oracle import _case_inputs
     g = golden("stage_cases.npz")
     for ci in range(int(g["ncases"][0])):
         s = _case_inputs(g, ci)
-        cell = gw.Cell(s["frus"].shape[0])
+        cell = gw.Cell(s["frus"].shape[0], fru_lanes=lanes)
         cell.upload(s)
         t0, tf = g["c%d_t" % ci]
         d0, df = g["c%d_dep" % ci]
@@ -81,11 +85,12 @@ def test_stage_cases_match_reference_fixture(gw):
         np.testing.assert_allclose(cell.avg_sums(), g["c%d_out_avg" % ci], rtol=RTOL, atol=1e-300)
 
 
+@pytest.mark.parametrize("lanes", LANES)
 @pytest.mark.parametrize("n", [1, 31, 129, 3001])
-def test_random_stages_match_oracle(gw, n):
+def test_random_stages_match_oracle(gw, n, lanes):
     rng = np.random.default_rng(n)
     s = _random_set(rng, n, 100 + n)
-    cell = gw.Cell(n)
+    cell = gw.Cell(n, fru_lanes=lanes)
     cell.upload(s)
     for k in range(6):
         v0 = rng.uniform(-100, 60)
@@ -103,10 +108,11 @@ def test_random_stages_match_oracle(gw, n):
     np.testing.assert_allclose(got["frus"], s["frus"], rtol=RTOL)
 
 
-def test_zero_length_stage_and_flux(gw):
+@pytest.mark.parametrize("lanes", LANES)
+def test_zero_length_stage_and_flux(gw, lanes):
     rng = np.random.default_rng(5)
     s = _random_set(rng, 200, 9)
-    cell = gw.Cell(200)
+    cell = gw.Cell(200, fru_lanes=lanes)
     cell.upload(s)
     dep = np.array([-85.0, 1e-4, 0.5])
     cur, num = cell.flux(dep)
@@ -117,13 +123,14 @@ def test_zero_length_stage_and_flux(gw):
     np.testing.assert_array_equal(got["frus"], s["frus"])
 
 
-def test_save_resume_restores_fru_and_rng_state(gw):
+@pytest.mark.parametrize("lanes", LANES)
+def test_save_resume_restores_fru_and_rng_state(gw, lanes):
     """send_save_state / send_resume_state (mpi_slave.c:150-226): a rejected
     step rolls FRUs and MT streams back, across MT regenerations."""
     n = 300
     rng = np.random.default_rng(3)
     s = _random_set(rng, n, 77)
-    cell = gw.Cell(n)
+    cell = gw.Cell(n, fru_lanes=lanes)
     cell.upload(s)
     d0 = np.array([-20.0, 3e-4, 0.9])
     df = np.array([-10.0, 3.2e-4, 0.88])
@@ -145,11 +152,12 @@ def test_save_resume_restores_fru_and_rng_state(gw):
     np.testing.assert_array_equal(first["frus"], second["frus"])
 
 
-def test_closed_loop_matches_reference_20ms(gw):
+@pytest.mark.parametrize("lanes", LANES)
+def test_closed_loop_matches_reference_20ms(gw, lanes):
     """The reference program at NFRU=250 (rest state, 1 Hz, seeds 5489+j):
     the GPU run reproduces its per-ms global states over the AP upstroke."""
     g = golden("closed250.npz")
-    cell = gw.Cell(250)
+    cell = gw.Cell(250, fru_lanes=lanes)
     st = gw.settings()
     state = cell.init_rest(st, scheme=gw.SEED_BASE, base=5489)
     _, states, other, cur = cell.run(state, 0.0, 20, set_=st)
@@ -160,10 +168,11 @@ def test_closed_loop_matches_reference_20ms(gw):
     assert np.mean(np.all(fin["ryr"].reshape(250, -1) == g["final_ryr"].reshape(250, -1), axis=1)) >= 0.99
 
 
-def test_gpu_runs_are_deterministic(gw):
+@pytest.mark.parametrize("lanes", LANES)
+def test_gpu_runs_are_deterministic(gw, lanes):
     outs = []
     for _ in range(2):
-        cell = gw.Cell(500)
+        cell = gw.Cell(500, fru_lanes=lanes)
         st = gw.settings()
         state = cell.init_rest(st, scheme=gw.SEED_BASE, base=1234)
         _, states, other, _ = cell.run(state, 5.0, 8, set_=st)
@@ -171,3 +180,22 @@ def test_gpu_runs_are_deterministic(gw):
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
     _same_ints(outs[0][2], outs[1][2])
+
+
+def test_stage_variants_agree(gw):
+    """Both stage kernels advance the same FRUs identically."""
+    rng = np.random.default_rng(17)
+    s = _random_set(rng, 4000, 5)
+    outs = []
+    for lanes in LANES:
+        cell = gw.Cell(4000, fru_lanes=lanes)
+        cell.upload(s)
+        nums = []
+        for k in range(4):
+            d0 = np.array([-60.0 + 20 * k, 2e-4, 0.7])
+            df = d0 + np.array([3.0, 1e-6, -0.001])
+            nums.append(cell.stage(0.01 * k, 0.01 * (k + 1), d0, df)[1])
+        outs.append((np.array(nums), cell.download()))
+    np.testing.assert_allclose(outs[0][0], outs[1][0], rtol=RTOL)
+    _same_ints(outs[0][1], outs[1][1])
+    np.testing.assert_array_equal(outs[0][1]["frus"], outs[1][1]["frus"])
