@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--step-ms", type=float, default=STEP_MS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--fru-lanes", type=int, default=4, choices=[1, 4],
                     help="lanes per FRU of the FP64 stage kernel (4: one per cleft, 1: one thread per FRU)")
     return ap.parse_args()
@@ -207,8 +208,8 @@ def run_reference(args, dist):
 # ---------------------------------------------------------------------------
 # GPU side
 # ---------------------------------------------------------------------------
-def fresh_cell(G, nfru, seed, lanes=4):
-    cell = G.Cell(nfru, fru_lanes=lanes)
+def fresh_cell(G, nfru, seed, lanes=4, precision="fp64"):
+    cell = G.Cell(nfru, fru_lanes=lanes, precision=precision)
     st = G.settings()
     state = cell.init_rest(st, scheme=G.SEED_BASE, base=seed)
     return cell, st, state
@@ -222,7 +223,7 @@ def run_gpu(args, dist):
     G.load()
     seed = SEED + dist.rank * args.nfru  # replicas: independent streams per rank
     # ---- device-resident run (value) ----
-    cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes)
+    cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, args.precision)
     t = 0.0
     oldstep = st.step_max
     for _ in range(args.warmup):
@@ -270,7 +271,7 @@ def run_gpu(args, dist):
     # ---- end to end through the C-ABI with host buffers (e2e) ----
     e2e = None
     if not args.no_e2e:
-        cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes)
+        cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, args.precision)
         t = 0.0
         oldstep = st.step_max
         for _ in range(args.warmup):
@@ -315,19 +316,21 @@ def run_gpu(args, dist):
             "metric": "cell-ms simulated/s at 12,500 FRUs", "value": value, "unit": "cell-ms/s",
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": wall_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
             "config": {"workload": "one cell per GPU, NFRU=%d, rest state, 1 Hz pacing (1 ms -100 uA/uF at 10 ms), "
                                    "seeds 5489+j; step = %g ms simulated; timed window [%g, %g) ms"
                                    % (args.nfru, args.step_ms, args.warmup * args.step_ms,
                                       (args.warmup + args.steps) * args.step_ms),
-                       "nfru": args.nfru, "step_ms": args.step_ms, "precision": "fp64 (FRU path and global ODE)",
+                       "nfru": args.nfru, "step_ms": args.step_ms, "precision": ("fp64 (FRU path and global ODE)" if args.precision == "fp64" else
+                                     "mixed (FRU rates and local Ca ODE fp32; FRU state, clock, flux sums and global ODE fp64)"),
                        "integrator": "host Dormand-Prince 5(4), FRU stages on GPU",
                        "fru_lanes": args.fru_lanes,
                        "l2": "flushed between timed steps (512 MB write)",
                        "parallelism": "replicas" if dist.world > 1 else "single GPU"},
             "fru_substeps": int(substeps), "fru_substeps_per_s": substeps / (wall_ms / 1000.0),
             "gpu_launches": int(launches),
-            "roofline": {"bound": "fp64", "kernel": "fru_stage4_kernel" if args.fru_lanes == 4 else "fru_stage_kernel", "achieved": achieved_tf,
+            "roofline": {"bound": "fp64", "kernel": ("fru_stage_mixed_kernel" if args.precision == "mixed" else
+                                                     "fru_stage4_kernel" if args.fru_lanes == 4 else "fru_stage_kernel"), "achieved": achieved_tf,
                          "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak if fp64_peak else None,
                          "peak_source": "measured in-run (independent DFMA chains on all SMs)",
                          "traffic": None, "per_launch_ms": per_launch_ms, "launches": int(kern_launches),

@@ -91,6 +91,8 @@ def bind(path):
         "gw_substeps": ([vp, P(C.c_ulonglong)], C.c_int),
         "gw_sync": ([vp], C.c_int),
         "gw_set_fru_lanes": ([vp, C.c_int], C.c_int),
+        "gw_set_precision": ([vp, C.c_int], C.c_int),
+        "gw_set_pca_scale": ([vp, C.c_double], C.c_int),
         "gw_settings_init": ([P(Settings)], None),
         "gw_rk54pd": ([vp, P(Settings), C.c_double, C.c_double, C.c_double, _dp, _dp, P(C.c_double)], C.c_int),
         "gw_lastcall": ([vp, P(Settings), C.c_double, _dp, _dp], C.c_int),
@@ -138,13 +140,17 @@ def _ptr(a):
 class Cell:
     """Device-resident FRU state of one cell (a gw_ctx)."""
 
-    def __init__(self, nfru, nfru_scale=None, lib=None, fru_lanes=None):
+    def __init__(self, nfru, nfru_scale=None, lib=None, fru_lanes=None, precision=None, pca_scale=None):
         self._L = L = lib if lib is not None else load()
         self._h = C.c_void_p()
         _check(L.gw_create(C.byref(self._h), int(nfru)), "gw_create", self._L)
         self.nfru = int(nfru)
         if nfru_scale is not None:
             _check(L.gw_set_scale(self._h, float(nfru_scale)), "gw_set_scale", self._L)
+        if precision is not None:
+            _check(L.gw_set_precision(self._h, 1 if precision in (1, "mixed") else 0), "gw_set_precision", self._L)
+        if pca_scale is not None:
+            _check(L.gw_set_pca_scale(self._h, float(pca_scale)), "gw_set_pca_scale", self._L)
         if fru_lanes is not None and hasattr(L, "gw_set_fru_lanes"):
             _check(L.gw_set_fru_lanes(self._h, int(fru_lanes)), "gw_set_fru_lanes", self._L)
 

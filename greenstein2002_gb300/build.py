@@ -24,6 +24,7 @@ CUDA_UNITS = {
     # source: extra flags
     "gw_fru_stage.cu": ["-fmad=false"],
     "gw_fru_stage4.cu": ["-fmad=false"],
+    "gw_fru_mixed.cu": [],
     "gw_abi.cu": [],
     "gw_probe.cu": [],
     "gw_noalloc.cu": ["-fmad=false"],

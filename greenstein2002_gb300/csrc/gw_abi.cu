@@ -50,9 +50,12 @@ struct gw_ctx {
   unsigned long long prof_launches = 0, launches = 0;
   void* flush_buf = nullptr;
   int fru_lanes = 4;        // lanes per FRU of the stage kernel: 1 or 4
+  int precision = 0;        // 0: FP64, 1: mixed (FP32 rates and local ODE)
+  double pca_scale = 1.0;   // LCC permeability scale of the cell
 };
 
 static cudaError_t launch_stage_variant(gw_ctx* c, const StageParams& p) {
+  if (c->precision == 1) return gw::launch_stage_mixed(c->d, p, c->stream);
   return c->fru_lanes == 4 ? gw::launch_stage4(c->d, p, c->stream) : gw::launch_stage(c->d, p, c->stream);
 }
 
@@ -147,7 +150,23 @@ extern "C" int gw_set_scale(gw_ctx* c, double nfru_scale) {
 
 extern "C" int gw_set_fru_lanes(gw_ctx* c, int lanes) {
   if (!c || (lanes != 1 && lanes != 4)) return set_err(GW_EINVAL, "gw_set_fru_lanes: lanes must be 1 or 4");
+  if (lanes == 1 && (c->precision != 0 || c->pca_scale != 1.0))
+    return set_err(GW_EINVAL, "gw_set_fru_lanes: the one-thread-per-FRU kernel is FP64 with the reference PCa only");
   c->fru_lanes = lanes;
+  return GW_OK;
+}
+
+extern "C" int gw_set_precision(gw_ctx* c, int precision) {
+  if (!c || (precision != 0 && precision != 1)) return set_err(GW_EINVAL, "gw_set_precision: 0 (FP64) or 1 (mixed)");
+  if (precision == 1 && c->fru_lanes == 1) c->fru_lanes = 4;
+  c->precision = precision;
+  return GW_OK;
+}
+
+extern "C" int gw_set_pca_scale(gw_ctx* c, double scale) {
+  if (!c || !(scale > 0.0)) return set_err(GW_EINVAL, "gw_set_pca_scale: scale must be > 0");
+  if (scale != 1.0 && c->fru_lanes == 1) c->fru_lanes = 4;
+  c->pca_scale = scale;
   return GW_OK;
 }
 
@@ -210,6 +229,7 @@ static int flush_pending(gw_ctx* c) {
   p.flags = c->pending;
   p.epoch = c->epoch;
   p.nfru_scale = c->nfru_scale;
+  p.pca_scale = c->pca_scale;
   c->pending = 0;
   CK(launch_stage_variant(c, p));
   c->launches++;
@@ -268,6 +288,7 @@ static int run_stage(gw_ctx* c, double t0, double tf, const double dep0[3], cons
     p.span[i] = depf[i] - dep0[i];
   }
   p.nfru_scale = c->nfru_scale;
+  p.pca_scale = c->pca_scale;
   p.epoch = c->epoch;
   p.flags = c->pending | (advance ? gw::kFlagAdvance : 0);
   c->pending = 0;

@@ -1,0 +1,568 @@
+// Cleft-parallel FRU substep loop, shared by the FP64 and the mixed-precision
+// stage kernels: each FRU is advanced by a group of four lanes, one per
+// dyadic cleft (8 FRUs per warp).
+//
+// Why four lanes per FRU: on GB300 every SM sub-partition issues one FP64
+// warp instruction per 64 cycles whatever the active-lane mask, so a stage
+// lasts as long as the FP64 instruction chain of its slowest FRU.  Spreading an
+// FRU over its clefts divides that chain by about four at the same total work.
+//
+// R = double: the plain FP64 method.  Every operation is the reference's, and
+// the arithmetic is arranged to issue few FP64 instructions while staying
+// bit-identical to it:
+//   - divisions by constants use Markstein's correction (q = x*r;
+//     q += fma(-q, d, x)*r), which returns the correctly rounded quotient;
+//   - max/min of non-negative doubles compare their bit patterns as integers;
+//   - channel exit totals come from per-state coefficient tables instead of
+//     divergent switches;
+//   - uniforms are compared with thresholds in the integer domain
+//     (u = y/2^32 > P  <=>  y > floor(P*2^32));
+//   - the four voltage exponentials of a substep are computed one per lane,
+//     and exp(2VF/RT) at the end of a substep is reused at the start of the
+//     next.
+// R = float: the mixed-precision method.  Transition rates and the local Ca
+// ODE are evaluated in FP32; FP64 is kept for the FRU Ca state itself (FP32
+// increments are accumulated in FP64), for the FRU clock and its step, and
+// for the cross-FRU flux sums.  Channel transitions use the complement form
+// 1 - u < dt*rate, which keeps full resolution near u = 1.
+//
+// Reference: simfru_local.c:32-278, fru_rates_local.c:30-798, fcn_fru.c:23-137,
+// mt19937_local.c:97-240.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gw_fru_core.cuh"
+#include "gw_fru_model.cuh"
+#include "gw_kernels.h"
+
+namespace gw {
+namespace cleft {
+
+// ---- type-specific operations ----------------------------------------------
+__device__ __forceinline__ long long ord(double a) { return __double_as_longlong(a); }
+__device__ __forceinline__ int ord(float a) { return __float_as_int(a); }
+// max/min of values known to be >= 0 (or of a negative value against a
+// positive constant): IEEE order equals the signed integer order of the bits;
+// ties return the first argument like the reference's macros
+template <typename R>
+__device__ __forceinline__ R imax(R a, R b) { return ord(a) < ord(b) ? b : a; }
+template <typename R>
+__device__ __forceinline__ R imin(R a, R b) { return ord(a) < ord(b) ? a : b; }
+template <typename R>
+__device__ __forceinline__ bool ilt(R a, R b) { return ord(a) < ord(b); }
+
+// x / d for a compile-time constant d with r = 1/d: correctly rounded in FP64
+__device__ __forceinline__ double divc(double x, double d, double r) {
+  const double q = x * r;
+  return fma(fma(-q, d, x), r, q);
+}
+__device__ __forceinline__ float divc(float x, float d, float r) { return x * r; }
+__device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double rexp(double x) { return exp(x); }
+__device__ __forceinline__ float rexp(float x) { return expf(x); }
+
+// FP64: u = y/2^32 compared with P = 1 - dt*R in the integer domain.
+__device__ __forceinline__ void thresh(double P, uint64_t& fl, bool& exact) {
+  const uint64_t b = (uint64_t)__double_as_longlong(P);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  const uint64_t M = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int sh = 20 - e;  // floor(P * 2^32) = M >> (52 - 32 - e)
+  if (sh >= 64) {
+    fl = 0;
+    exact = false;
+  } else {
+    fl = M >> sh;
+    exact = (M & ((1ull << sh) - 1ull)) == 0ull;
+  }
+}
+// leaves its state when u > 1 - dt*R (LCC, RyR) ...
+__device__ __forceinline__ bool leave_gt(uint32_t y, double dt, double R) {
+  const double P = 1.0 - dt * R;
+  if (P <= 0.0) return true;  // never on valid input (dt*rate <= 0.1)
+  uint64_t fl;
+  bool ex;
+  thresh(P, fl, ex);
+  return (uint64_t)y > fl;
+}
+// ... or when u >= 1 - dt*R (VDI gate, Cl channel)
+__device__ __forceinline__ bool leave_ge(uint32_t y, double dt, double R) {
+  const double P = 1.0 - dt * R;
+  if (P <= 0.0) return true;
+  uint64_t fl;
+  bool ex;
+  thresh(P, fl, ex);
+  return (uint64_t)y > fl || (ex && (uint64_t)y == fl);
+}
+// FP32: complement form, 1 - u = (2^32 - y)/2^32 against dt*R
+__device__ __forceinline__ bool leave_gt(uint32_t y, float dt, float R) {
+  return (float)(4294967296ull - (uint64_t)y) < dt * R * 4294967296.0f;
+}
+__device__ __forceinline__ bool leave_ge(uint32_t y, float dt, float R) {
+  return (float)(4294967296ull - (uint64_t)y) <= dt * R * 4294967296.0f;
+}
+
+// LCC exit total = (cX*bX + cY*bY) + cZ*bZ with bases {1, alpha, beta,
+// gamma, alpha', beta'}: the sums of fru_rates_local.c:176-340 in their order.
+__constant__ double c_lcc_coef[13][3] = {
+    {0.0, 0.0, 0.0},
+    {4.0, 1.0, 0.0},                     // 1: 4a + g
+    {1.0, 3.0, aL},                      // 2: b + 3a + aL g
+    {2.0, 2.0, aL * aL},                 // 3
+    {3.0, 1.0, aL * aL * aL},            // 4
+    {4.0, fL, aL * aL * aL * aL},        // 5
+    {gL, 0.0, 0.0},                      // 6
+    {4.0, CCa0_to_C0, 0.0},              // 7: 4a' + omega
+    {1.0, 3.0, CCa1_to_C1},              // 8: b' + 3a' + omega/bL
+    {2.0, 2.0, CCa2_to_C2},              // 9
+    {3.0, 1.0, CCa3_to_C3},              // 10
+    {4.0, CCa4_to_C4, fLprime},          // 11
+    {gLprime, 0.0, 0.0},                 // 12
+};
+// basis index of each term, packed 3 x 4 bits per state:
+// 0 = 1, 1 = alpha, 2 = beta, 3 = gamma, 4 = alpha', 5 = beta'
+__constant__ uint16_t c_lcc_basis[13] = {
+    0x000, 0x031, 0x312, 0x312, 0x312, 0x302, 0x000, 0x004, 0x045, 0x045, 0x045, 0x005, 0x000,
+};
+
+template <typename R>
+__device__ __forceinline__ R pick_basis(int i, R al, R be, R ga, R ap, R bp) {
+  R v = R(1);
+  v = (i == 1) ? al : v;
+  v = (i == 2) ? be : v;
+  v = (i == 3) ? ga : v;
+  v = (i == 4) ? ap : v;
+  v = (i == 5) ? bp : v;
+  return v;
+}
+
+struct Group {
+  int c;           // cleft of this lane (0..3)
+  int base;        // lane index of cleft 0 of this FRU within the warp
+  unsigned mask;   // the four lanes of this FRU
+};
+
+// group-local shuffles (the four lanes of one FRU may run while other
+// groups of the warp have finished their substeps)
+template <typename T>
+__device__ __forceinline__ T from(const Group& g, T v, int c) {
+  return __shfl_sync(g.mask, v, g.base + c);
+}
+template <typename R>
+__device__ __forceinline__ R gmax(const Group& g, R v) {
+  v = imax(v, __shfl_xor_sync(g.mask, v, 1));
+  v = imax(v, __shfl_xor_sync(g.mask, v, 2));
+  return v;
+}
+
+// Cooperative in-place regeneration of an FRU's 624 words by its 4 lanes, in
+// chunks of 4 consecutive words.  Words k >= 227 depend on words the same
+// regeneration produced 227 positions earlier (other lanes), so the group
+// synchronises after every chunk.
+__device__ __forceinline__ void regen4(uint32_t* m, const Group& g) {
+  for (int k0 = 0; k0 < kMtN; k0 += 4) {
+    const int k = k0 + g.c;
+    const uint32_t cur = m[k];
+    const uint32_t nxt = m[(k + 1 == kMtN) ? 0 : k + 1];
+    const uint32_t far = m[(k + kMtM) % kMtN];
+    __syncwarp(g.mask);
+    const uint32_t y = (cur & 0x80000000u) | (nxt & 0x7fffffffu);
+    m[k] = far ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+    __syncwarp(g.mask);
+  }
+}
+__device__ __forceinline__ void copy4(uint32_t* dst, const uint32_t* src, const Group& g) {
+  for (int k = g.c; k < kMtN; k += 4) dst[k] = src[k];
+  __syncwarp(g.mask);
+}
+
+struct StageCtx {
+  const StageParams* p;
+  uint32_t* m;          // MT row of this FRU
+  uint32_t* hold;       // copy-on-twist row
+  uint32_t* hold_epoch;
+};
+
+// Fetch the words of one substep: E_tot extra draws (lane c owns positions
+// pre .. pre+ne-1) followed by the 32 batch draws (lane c owns 8c .. 8c+7),
+// regenerating the row in between when the stream crosses word 624.
+__device__ __forceinline__ void fetch_words(const StageCtx& sc, const Group& g, int& mti, int pre, int ne, int etot,
+                                            uint32_t ex[kRyR], uint32_t bw[8]) {
+  const int W = etot + 32;
+  const bool cross = (mti + W > kMtN);
+  int pos;
+  // old generation first
+#pragma unroll
+  for (int i = 0; i < kRyR; i++) {
+    pos = mti + pre + i;
+    if (i < ne && pos < kMtN) ex[i] = sc.m[pos];
+  }
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    pos = mti + etot + 8 * g.c + k;
+    if (pos < kMtN) bw[k] = sc.m[pos];
+  }
+  if (cross) {
+    const bool need_copy = *sc.hold_epoch != sc.p->epoch;
+    __syncwarp(g.mask);  // every lane has read its old words and the epoch
+    if (need_copy) {
+      copy4(sc.hold, sc.m, g);
+      if (g.c == 0) *sc.hold_epoch = sc.p->epoch;
+    }
+    regen4(sc.m, g);
+#pragma unroll
+    for (int i = 0; i < kRyR; i++) {
+      pos = mti + pre + i;
+      if (i < ne && pos >= kMtN) ex[i] = sc.m[pos - kMtN];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      pos = mti + etot + 8 * g.c + k;
+      if (pos >= kMtN) bw[k] = sc.m[pos - kMtN];
+    }
+    mti = mti + W - kMtN;
+  } else {
+    mti = mti + W;
+  }
+#pragma unroll
+  for (int i = 0; i < kRyR; i++) ex[i] = mt_temper(ex[i]);
+#pragma unroll
+  for (int k = 0; k < 8; k++) bw[k] = mt_temper(bw[k]);
+}
+
+// Local Ca ODE of one cleft (fcn_fru.c:23-137) evaluated by the FRU's four
+// lanes.  Each lane returns dCaSS of its cleft; every lane returns the same
+// dCaJSR.  e2 = exp(2 V F/RT) and a2j are passed in (shared by all lanes).
+template <typename R>
+__device__ __forceinline__ void fcn_fru4(const Group& g, R cajsr, R cass, const R dep[3], R e2, R a2j, bool small,
+                                         R lopen, int nopen, R pca_scale, R& dJSR, R& dSS) {
+  constexpr double JDHconstant = 1.0 / (2.0 * VSS * Faraday * 1000.0);
+  constexpr double KJDHsmall = -PCa * 2.0 * 1000.0 * Faraday;
+  const R Cai = dep[1], CaNSR = dep[2];
+  // JRyR of every cleft, summed in cleft order
+  const R jcoef = R(JRyRmax) * (R)nopen;
+  const R JRyR = jcoef * (cajsr - cass);
+  const R j0 = from(g, JRyR, 0), j1 = from(g, JRyR, 1), j2 = from(g, JRyR, 2), j3 = from(g, JRyR, 3);
+  const R JRyRtot = j0 + j1 + j2 + j3;
+  const R cnext = from(g, cass, (g.c + 1) & 3);
+  const R Jss = divc(cass - cnext, R(tauss2ss), R(1.0 / tauss2ss));
+  const R Jss_prev = from(g, Jss, (g.c + 3) & 3);
+  const R Jxfer = divc(cass - Cai, R(tauxfer), R(1.0 / tauxfer));
+  const R JDH = small ? R(KJDHsmall) * pca_scale * (cass - R(Cao * 0.341)) * lopen * R(JDHconstant)
+                      : -(cass * e2 - R(Cao * 0.341)) * a2j * lopen;
+  R a1 = rdiv(R(BSRtot * KBSR), (cass + R(KBSR)) * (cass + R(KBSR)));
+  R a2 = rdiv(R(BSLtot * KBSL), (cass + R(KBSL)) * (cass + R(KBSL)));
+  const R bSS = rdiv(R(1), R(1) + a1 + a2);
+  dSS = bSS * (JDH + JRyR - Jxfer - Jss + Jss_prev);
+  const R Jtr = divc(CaNSR - cajsr, R(tautr), R(1.0 / tautr));
+  a1 = rdiv(R(CSQNtot * KmCSQN), (cajsr + R(KmCSQN)) * (cajsr + R(KmCSQN)));
+  const R bJSR = rdiv(R(1), R(1) + a1);
+  dJSR = bJSR * (Jtr - R(VSS / VJSR) * JRyRtot);
+}
+
+// exp(2 V F / RT) and the GHK factor a2 of fcn_fru.c:78-101 for voltage V
+template <typename R>
+__device__ __forceinline__ void ghk_terms(R V, R pca_scale, R& e2, R& a2j, bool& small) {
+  constexpr double JDHconstant = 1.0 / (2.0 * VSS * Faraday * 1000.0);
+  const R VFRT = divc(V, R(RT_over_F), R(1.0 / RT_over_F));
+  const R VFsqRT = R(1000.0 * Faraday) * VFRT;
+  e2 = rexp(R(2) * VFRT);
+  small = fabs(V) < R(1.e-6);
+  a2j = small ? R(0) : rdiv(R(PCa * 4.0) * pca_scale * VFsqRT, e2 - R(1)) * R(JDHconstant);
+}
+
+__device__ __forceinline__ double frac_of(double t, double t0, double interval, double) { return (t - t0) / interval; }
+__device__ __forceinline__ float frac_of(double t, double t0, double, float rinterval) {
+  return (float)(t - t0) * rinterval;
+}
+
+// One FRU over [t0, tf] by its four lanes (simfru_local.c:83-277).  cajsr and
+// cass are the FRU's FP64 state; arithmetic runs in R.
+template <typename R>
+__device__ __forceinline__ void advance4(const StageCtx& sc, const Group& g, double& cajsr64, double& cass64,
+                                         uint32_t& w, int& mti, uint32_t& nsub, bool& overflow) {
+  const StageParams& p = *sc.p;
+  R dep0[3], span[3], dep[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    dep0[i] = (R)p.dep0[i];
+    span[i] = (R)p.span[i];
+    dep[i] = dep0[i];
+  }
+  const R pca_scale = (R)p.pca_scale;
+  R lopen = lcc_open(w) ? R(1) : R(0);
+  int nopen = ryr_open_count(w);
+  const double interval = p.tf - p.t0;
+  const R rinterval = (R)(1.0 / interval);
+  double t = p.t0;
+  R e2, a2j;
+  bool small;
+  ghk_terms(dep[0], pca_scale, e2, a2j, small);
+  // per-lane voltage exponential of the rates: alpha, beta, yCa_inf, tau_yCa
+  //   lane 0: alphacf*exp(0.012*(V-35))     lane 1: betacf*exp(-0.05*(V-35))
+  //   lane 2: 0.4/(1+exp((V+12.5)/5)) + 0.6  lane 3: 60 + 340/(1+exp((V+30)/12))
+  const bool isdiv = g.c >= 2;
+  const R cA = isdiv ? (g.c == 2 ? R(12.5) : R(30.0)) : R(-35.0);
+  const R cR = isdiv ? (g.c == 2 ? R(1.0 / 5.0) : R(1.0 / 12.0)) : (g.c == 0 ? R(0.012) : R(-0.05));
+  const R cD = isdiv ? (g.c == 2 ? R(5.0) : R(12.0)) : R(1.0);
+  const R cCF = isdiv ? R(0.0) : (g.c == 0 ? R(alphacf) : R(betacf));
+  const R cK = isdiv ? (g.c == 2 ? R(0.4) : R(340.0)) : R(1.0);
+  const R cM = isdiv ? (g.c == 2 ? R(1.0 - 0.4) : R(60.0)) : R(0.0);
+  while (true) {
+    // the loop condition is uniform over the group (t is the same in all four lanes)
+    if (!(t < p.tf)) break;
+    if (nsub >= (1u << 22)) {
+      overflow = true;
+      break;
+    }
+    const R cajsr = (R)cajsr64, cass = (R)cass64;
+    // ---- voltage terms at the substep start, one exponential per lane ----
+    const R x = dep[0] + cA;
+    R q = x * cR;
+    if (isdiv) q = divc(x, cD, cR);
+    const R ev = rexp(q);
+    const R r01 = cCF * ev;
+    const R r23 = rdiv(cK, R(1) + ev) + cM;
+    const R vterm = isdiv ? r23 : r01;
+    const R alpha = from(g, vterm, 0), beta = from(g, vterm, 1);
+    const R yinf = from(g, vterm, 2), tau = from(g, vterm, 3);
+    const R bp = divc(beta, R(bL * kappa), R(1.0 / (bL * kappa)));
+    const R ap = R(aL) * alpha;
+    // ---- exit totals of this cleft's 8 channels ----
+    const R gam = R(gammacf) * cass;
+    R R0[8];
+    {
+      const int s = lcc_of(w);
+      const uint16_t bi = c_lcc_basis[s];
+      const R X = R(c_lcc_coef[s][0]) * pick_basis(bi & 15, alpha, beta, gam, ap, bp);
+      const R Y = R(c_lcc_coef[s][1]) * pick_basis((bi >> 4) & 15, alpha, beta, gam, ap, bp);
+      const R Z = R(c_lcc_coef[s][2]) * pick_basis((bi >> 8) & 15, alpha, beta, gam, ap, bp);
+      R0[0] = X + Y + Z;
+    }
+    {
+      const R num = (vdi_of(w) == 2) ? (R(1) - yinf) : yinf;
+      R0[1] = rdiv(num, tau);
+    }
+    // RyR constants of the cleft and the pseudo-state draws
+    const R c2 = cass * cass;
+    const R sat = imin(R(threshMAX), divc(c2, R(k_rate), R(1.0 / k_rate)));
+    const R sat2 = imin(R(threshMAX), divc(c2, R(k_rate2), R(1.0 / k_rate2)));
+    const R k12 = R(k12cf) * sat2, k23 = R(k23cf) * sat, k34 = R(k34cf) * sat;
+    const R k54 = R(k54cf) * sat, k25 = R(k25cf) * sat, k56 = R(k56cf) * sat;
+    int regime;
+    {
+      const R cc = imin(cass, R(threshMAXCa));
+      regime = ilt(cc, R(threshCa56to8)) ? 0 : (ilt(cc, R(threshCa34to7)) ? 1 : 2);
+    }
+    // extra draws: regime 0 resolves 7 and 8, regime 1 resolves 7 (in cleft, then RyR order)
+    int ne = 0;
+#pragma unroll
+    for (int i = 0; i < kRyR; i++) {
+      const int s = ryr_of(w, i);
+      ne += (regime == 0 && (s == 7 || s == 8)) || (regime == 1 && s == 7);
+    }
+    const int n0 = from(g, ne, 0), n1 = from(g, ne, 1), n2 = from(g, ne, 2), n3 = from(g, ne, 3);
+    const int pre = (g.c > 0 ? n0 : 0) + (g.c > 1 ? n1 : 0) + (g.c > 2 ? n2 : 0);
+    const int etot = n0 + n1 + n2 + n3;
+    uint32_t exw[kRyR] = {0u, 0u, 0u, 0u, 0u}, bw[8];
+    fetch_words(sc, g, mti, pre, ne, etot, exw, bw);
+    {
+      int used = 0;
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) {
+        int s = ryr_of(w, i);
+        if (regime == 0) {
+          if (s == 7 || s == 8) {
+            const double u = (double)exw[used++] / 4294967296.0;
+            if (s == 7) s = (u < (double)(k34 / (k34 + R(k43)))) ? 4 : 3;
+            else s = (u < (double)(k56 / (k56 + R(k65)))) ? 6 : 5;
+          }
+        } else if (regime == 1) {
+          if (s == 7) {
+            const double u = (double)exw[used++] / 4294967296.0;
+            s = (u < (double)(k34 / (k34 + R(k43)))) ? 4 : 3;
+          }
+          if (s == 5 || s == 6) s = 8;
+        } else {
+          if (s == 3 || s == 4) s = 7;
+          else if (s == 5 || s == 6) s = 8;
+        }
+        w = set_field(w, 8 + 4 * i, s);
+      }
+    }
+    {
+      bool need7 = false, need8 = false;
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) {
+        const int s = ryr_of(w, i);
+        need7 |= (s == 7);
+        need8 |= (s == 8);
+      }
+      const R T2 = R(k21) + k23 + k25, T3 = R(k32) + k34, T5 = R(k52) + k54 + k56;
+      const R T4 = R(k43 + k45);
+      R T7 = R(0), T8 = R(0);
+      if (need7) {
+        const R a1 = k34 / (R(k43) + k34);
+        T7 = (R(1) - a1) * R(k32) + a1 * R(k45);
+      }
+      if (need8) {
+        const R a1 = R(k65) / (k56 + R(k65));
+        T8 = a1 * R(k52) + a1 * k54;
+      }
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) {
+        const int s = ryr_of(w, i);
+        R r = k12;
+        r = (s == 2) ? T2 : r;
+        r = (s == 3) ? T3 : r;
+        r = (s == 4) ? T4 : r;
+        r = (s == 5) ? T5 : r;
+        r = (s == 6) ? R(k65) : r;
+        r = (s == 7) ? T7 : r;
+        r = (s == 8) ? T8 : r;
+        R0[2 + i] = r;
+      }
+    }
+    R0[7] = (cl_of(w) == 1) ? R(kfIto2) * cass : R(kbIto2);
+    R mx = R(0);
+#pragma unroll
+    for (int j = 0; j < 8; j++) mx = imax(mx, R0[j]);
+    mx = gmax(g, mx);
+    // ---- substep size (simfru_local.c:135-146) ----
+    R dtr = imin(rdiv(R(0.1), mx), R(10.001e-3));
+    const R cmax = gmax(g, imax(R(0.e-3), cass));
+    if (cmax > R(1.5e-3)) dtr = imin(dtr, R(5.001e-3));
+    const double dt64 = imin((double)dtr, p.tf - t);
+    const R dt = (R)dt64;
+    // ---- Heun step (simfru_local.c:149-173) ----
+    R dJ, dS;
+    fcn_fru4(g, cajsr, cass, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
+    const R k1J = dt * dJ, k1S = dt * dS;
+    const R y1J = cajsr + k1J, y1S = cass + k1S;
+    t = t + dt64;
+    const R frac = frac_of(t, p.t0, interval, rinterval);
+#pragma unroll
+    for (int i = 0; i < 3; i++) dep[i] = dep0[i] + frac * span[i];
+    ghk_terms(dep[0], pca_scale, e2, a2j, small);
+    fcn_fru4(g, y1J, y1S, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
+    cajsr64 = cajsr64 + (double)((k1J + dt * dJ) / R(2));
+    cass64 = cass64 + (double)((k1S + dt * dS) / R(2));
+    // ---- transitions of this cleft's 8 channels (:215-276) ----
+    bool moved = false;
+    if (leave_gt(bw[0], dt, R0[0])) {
+      const LccBasis lb{(double)alpha, (double)beta, (double)bp};
+      double r[4];
+      int d[4];
+      const int len = lcc_row(lcc_of(w), lb, (double)gam, r, d);
+      w = set_field(w, 0, pick_dest(r, d, len, (double)dt, (double)bw[0] / 4294967296.0));
+    }
+    if (leave_ge(bw[1], dt, R0[1])) w = set_field(w, 4, 3 - vdi_of(w));
+#pragma unroll
+    for (int i = 0; i < kRyR; i++) {
+      if (leave_gt(bw[2 + i], dt, R0[2 + i])) {
+        RyrK k;
+        k.k12 = k12;
+        k.k23 = k23;
+        k.k34 = k34;
+        k.k54 = k54;
+        k.k25 = k25;
+        k.k56 = k56;
+        k.regime = regime;
+        double r[4];
+        int d[4];
+        const int len = ryr_row(ryr_of(w, i), k, r, d);
+        w = set_field(w, 8 + 4 * i, pick_dest(r, d, len, (double)dt, (double)bw[2 + i] / 4294967296.0));
+        moved = true;
+      }
+    }
+    if (leave_ge(bw[7], dt, R0[7])) w = set_field(w, 28, 3 - cl_of(w));
+    lopen = lcc_open(w) ? R(1) : R(0);
+    if (moved) nopen = ryr_open_count(w);
+    nsub++;
+  }
+}
+
+// The stage kernel: load, optional snapshot save/restore, advance, store,
+// and the fused deterministic flux reduction (calc_fru_flux_local.c:28-77,
+// mpi_master.c:447-468, mpi_slave.c:150-226).
+template <typename R>
+__device__ __forceinline__ void stage_body(DevState& s, const StageParams& p) {
+  __shared__ double smem[32 * 5];
+  const int lane = threadIdx.x & 31;
+  Group g;
+  g.c = lane & 3;
+  g.base = lane & ~3;
+  g.mask = 0xfu << g.base;
+  const int f = blockIdx.x * 8 + (threadIdx.x >> 2);
+  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  uint32_t nsub = 0;
+  bool overflow = false;
+  const bool active = f < s.nfru;  // uniform over each 4-lane group
+  if (active) {
+    const size_t nf = (size_t)s.stride;
+    double cajsr, cass;
+    uint32_t w;
+    int mti;
+    StageCtx sc;
+    sc.p = &p;
+    sc.m = s.mt + (size_t)f * kMtStride;
+    sc.hold = s.mt_hold + (size_t)f * kMtStride;
+    sc.hold_epoch = s.hold_epoch + f;
+    if (p.flags & kFlagResume) {
+      cajsr = s.frus_s[f];
+      cass = s.frus_s[(g.c + 1) * nf + f];
+      w = s.chan_s[g.c * nf + f];
+      mti = s.mti_s[f];
+      if (*sc.hold_epoch == p.epoch) copy4(sc.m, sc.hold, g);
+    } else {
+      cajsr = s.frus[f];
+      cass = s.frus[(g.c + 1) * nf + f];
+      w = s.chan[g.c * nf + f];
+      mti = s.mti[f];
+    }
+    if (p.flags & kFlagSave) {
+      if (g.c == 0) {
+        s.frus_s[f] = cajsr;
+        s.mti_s[f] = mti;
+      }
+      s.frus_s[(g.c + 1) * nf + f] = cass;
+      s.chan_s[g.c * nf + f] = w;
+    }
+    if (p.flags & kFlagAdvance) advance4<R>(sc, g, cajsr, cass, w, mti, nsub, overflow);
+    if (g.c == 0) {
+      s.frus[f] = cajsr;
+      s.mti[f] = mti;
+    }
+    s.frus[(g.c + 1) * nf + f] = cass;
+    s.chan[g.c * nf + f] = w;
+    v[0] = cass;
+    v[1] = (g.c == 0) ? cajsr : 0.0;
+    if (lcc_open(w)) {
+      v[2] = cass;
+      v[3] = 1.0;
+    }
+    if (cl_of(w) == 2) v[4] = 1.0;
+  }
+  __syncwarp();
+  if (overflow) s.out[kOutError] = 1.0;
+  if (s.substeps) {
+    unsigned long long c = (g.c == 0) ? nsub : 0;
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if (lane == 0 && c) atomicAdd(s.substeps, c);
+  }
+  block_reduce<5>(v, smem);
+  double tot[5];
+  if (grid_finish<5>(v, s.partials, s.ticket, smem, tot)) {
+    double cur[4];
+    currents_from_sums(s.nfru, p.nfru_scale, p.depf, tot, cur);
+    cur[2] = cur[2] * p.pca_scale;  // ICa is proportional to the LCC permeability
+#pragma unroll
+    for (int k2 = 0; k2 < 5; k2++) s.out[k2] = tot[k2];
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) s.out[5 + k2] = cur[k2];
+  }
+}
+
+}  // namespace cleft
+}  // namespace gw

@@ -1,0 +1,22 @@
+// Mixed-precision cleft-parallel FRU stage kernel: transition rates and the
+// FRU-local Ca ODE in FP32 (FP32 issues 64x faster than FP64 on GB300); the
+// FRU Ca state, the FRU clock, its step and the cross-FRU flux sums stay FP64.
+// The channel algorithm, its MT19937 draw order and the transition rules are
+// the FP64 method's (gw_fru_cleft.cuh), so both share every random number.
+//
+// Reference: simfru_local.c:32-278, fru_rates_local.c:30-798, fcn_fru.c:23-137.
+#include "gw_fru_cleft.cuh"
+
+namespace gw {
+
+__global__ void __launch_bounds__(32) fru_stage_mixed_kernel(DevState s, StageParams p) {
+  cleft::stage_body<float>(s, p);
+}
+
+cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, cudaStream_t st) {
+  const int blocks = (s.nfru + 7) / 8;
+  fru_stage_mixed_kernel<<<blocks, 32, 0, st>>>(s, p);
+  return cudaGetLastError();
+}
+
+}  // namespace gw

@@ -49,13 +49,16 @@ struct StageParams {
   double t0, tf;
   double dep0[3], span[3], depf[3];
   double nfru_scale;
+  double pca_scale;  // LCC permeability scale of the cell (1 = reference PCa)
   uint32_t epoch;
   int flags;
 };
 
 cudaError_t launch_stage(const DevState& s, const StageParams& p, cudaStream_t st);
-// cleft-parallel variant: 4 lanes per FRU, 8 FRUs per single-warp block
+// cleft-parallel variants: 4 lanes per FRU, 8 FRUs per single-warp block;
+// FP64 (the plain method) and mixed precision (FP32 rates and local ODE)
 cudaError_t launch_stage4(const DevState& s, const StageParams& p, cudaStream_t st);
+cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, cudaStream_t st);
 cudaError_t launch_avg(const DevState& s, cudaStream_t st);
 // FP64 FMA throughput of the device (TFLOP/s, best of a few launches).
 cudaError_t probe_fp64(int sms, double* tflops);

@@ -84,6 +84,15 @@ int gw_resume(gw_ctx *ctx);
  * FRUs per warp.  Results are identical; the choice only changes speed. */
 int gw_set_fru_lanes(gw_ctx *ctx, int lanes);
 
+/* Arithmetic of the FRU path: 0 (default) = FP64, the plain method;
+ * 1 = mixed precision: transition rates and the FRU-local Ca ODE in FP32,
+ * FP64 kept for the FRU Ca state, the FRU clock and the flux sums.  Both use
+ * the same channel algorithm and the same MT19937 draws. */
+int gw_set_precision(gw_ctx *ctx, int precision);
+/* Per-cell scale of the LCC permeability PCa (g_CaL; 1.0 = the reference,
+ * parameters_fcn_fru.c:48), applied to the LCC flux of every cleft and to ICa. */
+int gw_set_pca_scale(gw_ctx *ctx, double scale);
+
 /* FRU-substeps executed since creation (workload counter). */
 int gw_substeps(gw_ctx *ctx, unsigned long long *count);
 /* Wait for all work of the context. */
