@@ -3,11 +3,18 @@
 Workload (the full-size plain FP64 configuration): one cell of NFRU=12,500
 release units, rest initial state (initialize_state.c:164-219), per-FRU
 MT19937 seeded 5489+j, 1 Hz pacing with a 1 ms -100 uA/uF stimulus at
-10 ms.  A step advances the cell by STEP_MS (50 ms) of simulated time through
+10 ms.  A step advances the cell by STEP_MS (10 ms) of simulated time through
 the whole hot path (Dormand-Prince global step, every FRU stage on the GPU).
-Warm-up steps cover [0, W*50) ms, so with the defaults (W=3, K=20) the timed
-window is [150, 1150) ms: one full pacing cycle including the second beat's
-upstroke.  L2 (129 MB) is flushed by a 512 MB write between timed steps.
+Warm-up steps cover [0, W*10) ms (the stimulus and upstroke), so with the
+defaults (W=3, K=20) the timed window is [30, 230) ms: the plateau of the
+first beat, when Ca release keeps the most FRUs busy -- more FRU-substeps per
+ms than the beat average, so the rate is a conservative one.  L2 (129 MB) is
+flushed by a 512 MB write between timed steps.
+
+Beside the FP64 value the line carries the same window in mixed precision
+("mixed", with its error against the FP64 run) and a batched run ("batched":
+many cells of NFRU 1250-12,500 with varied pacing and conductances sharing
+each stage launch, mixed precision).
 
 value: inputs resident in HBM, device-timed with CUDA events on the library's
 stream.  e2e: the same window through the C-ABI with host buffers: every
@@ -31,7 +38,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 NFRU = 12500
-STEP_MS = 50.0
+STEP_MS = 10.0
 SEED = 5489
 # algorithmic work per FRU-substep (static count of the reference's substep:
 # fru_rates_local + 2 x fcn_fru + simfru_local body, each add/mul/div/exp/
@@ -51,6 +58,19 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-cells", type=int, default=64)
+    ap.add_argument("--batch-ms", type=int, default=20)
+    ap.add_argument("--batch-warmup-ms", type=int, default=10)
+    ap.add_argument("--batch-mode", default="streams", choices=["streams", "lockstep"],
+                    help="streams: each cell on its own stream; lockstep: shared batched launches")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[10.0, 50.0, 200.0])
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-ms", type=float, default=20.0)
+    ap.add_argument("--serve-slots", type=int, default=32)
+    ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--fru-lanes", type=int, default=4, choices=[1, 4],
                     help="lanes per FRU of the FP64 stage kernel (4: one per cleft, 1: one thread per FRU)")
     return ap.parse_args()
@@ -215,6 +235,178 @@ def fresh_cell(G, nfru, seed, lanes=4, precision="fp64"):
     return cell, st, state
 
 
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
+    """Device-resident run of one cell: warm-up, then K timed steps with CUDA
+    events on the library's stream.  Returns the measurements."""
+    import numpy as np
+    cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, precision)
+    t = 0.0
+    oldstep = st.step_max
+    n = int(args.step_ms)
+    for _ in range(args.warmup):
+        t, _, _, _ = cell.run(state, t, n, oldstep, st, want=())
+        oldstep = cell.oldstep
+    sub0, launch0 = cell.substeps(), cell.launches()
+    cell.profile(True)
+    total_ms = 0.0
+    trace = []
+    dist.barrier()
+    cell.sync()
+    if clocks:
+        clocks.start()
+    for _ in range(args.steps):
+        cell.l2_flush()
+        cell.event(0)
+        t, states, _, _ = cell.run(state, t, n, oldstep, st, want=("states",) if keep_trace else ())
+        oldstep = cell.oldstep
+        cell.event(1)
+        total_ms += cell.elapsed_ms(0, 1)
+        if keep_trace:
+            trace.append(states)
+    cell.sync()
+    clk = clocks.stop() if clocks else None
+    dist.barrier()
+    kern_ms, kern_launches = cell.profile_read()
+    out = {"wall_ms": dist.max(total_ms), "substeps": cell.substeps() - sub0, "launches": cell.launches() - launch0,
+           "kern_ms": kern_ms, "kern_launches": kern_launches, "clocks": clk,
+           "trace": np.concatenate(trace) if keep_trace else None}
+    out["value"] = dist.sum(args.steps * args.step_ms) / (out["wall_ms"] / 1000.0)
+    cell.close()
+    return out
+
+
+def time_e2e(G, args, dist, seed):
+    """The same window through the C-ABI with host buffers: the cell's full FRU +
+    RNG state is uploaded and downloaded, and its traces read back, every step."""
+    cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, args.precision)
+    t = 0.0
+    oldstep = st.step_max
+    n = int(args.step_ms)
+    for _ in range(args.warmup):
+        t, _, _, _ = cell.run(state, t, n, oldstep, st, want=())
+        oldstep = cell.oldstep
+    host = cell.download()
+    h_state = state.copy()
+    h2d = sum(v.nbytes for v in host.values()) + h_state.nbytes
+    dist.barrier()
+    cell.sync()
+    e2e_ms, d2h = 0.0, 0
+    for _ in range(args.steps):
+        cell.l2_flush()
+        t0 = time.perf_counter()
+        cell.upload(host)
+        t, states, other, cur = cell.run(h_state, t, n, oldstep, st)
+        oldstep = cell.oldstep
+        host = cell.download()
+        e2e_ms += (time.perf_counter() - t0) * 1000.0
+        d2h = sum(v.nbytes for v in host.values()) + states.nbytes + other.nbytes + cur.nbytes
+    dist.barrier()
+    cell.close()
+    return {"value": dist.sum(args.steps * args.step_ms) / (dist.max(e2e_ms) / 1000.0), "unit": "cell-ms/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+
+def time_batched(G, args, dist):
+    """Many cells sharing each stage launch (gw_batch), mixed precision: NFRU drawn
+    from {1250, 2500, 5000, 12500}, pacing cycle length U(300, 2000) ms, PCa and
+    GKr scaled by lognormal(0, 0.2) factors; one host thread per cell."""
+    import numpy as np
+    rng = np.random.default_rng(20021 + dist.rank)
+    n = args.batch_cells
+    sizes = rng.choice([1250, 2500, 5000, 12500], n)
+    cells, sets, states = [], [], []
+    for i in range(n):
+        pca, gkr = np.exp(rng.normal(0.0, 0.2, 2))
+        c = G.Cell(int(sizes[i]), precision="mixed", pca_scale=float(pca))
+        st = G.settings(period=float(rng.uniform(300.0, 2000.0)), scale_GKr=float(gkr))
+        states.append(c.init_rest(st, scheme=G.SEED_BASE, base=SEED + 100003 * i))
+        cells.append(c)
+        sets.append(st)
+    states = np.ascontiguousarray(np.array(states))
+    t = np.zeros(n)
+    old = np.full(n, 0.1)
+    b = G.Batch("mixed")
+    lock = args.batch_mode == "lockstep"
+    b.run(cells, sets, t, states, old, args.batch_warmup_ms, lockstep=lock)
+    sub0 = sum(c.substeps() for c in cells)
+    b.profile(True)
+    launch0 = sum(c.launches() for c in cells)
+    dist.barrier()
+    t0 = time.perf_counter()
+    b.run(cells, sets, t, states, old, args.batch_ms, lockstep=lock)
+    wall = time.perf_counter() - t0
+    kern_ms, launches = b.profile(False)
+    if not lock:
+        kern_ms, launches = None, sum(c.launches() for c in cells) - launch0
+    substeps = sum(c.substeps() for c in cells) - sub0
+    cell_ms = n * args.batch_ms
+    eq_ms = float(np.sum(sizes)) / NFRU * args.batch_ms
+    for c in cells:
+        c.close()
+    b.close()
+    return {"value": dist.sum(cell_ms) / dist.max(wall), "unit": "cell-ms/s (cells of mixed NFRU)",
+            "value_12500_equiv": dist.sum(eq_ms) / dist.max(wall), "cells": n,
+            "nfru_mix": {str(k): int(np.sum(sizes == k)) for k in (1250, 2500, 5000, 12500)},
+            "window_ms": [args.batch_warmup_ms, args.batch_warmup_ms + args.batch_ms],
+            "fru_substeps_per_s": substeps / wall, "batched_launches": int(launches),
+            "kernel_ms": kern_ms, "precision": "mixed", "mode": args.batch_mode,
+            "timing": "host wall clock around the batched run (one host thread per cell)"}
+
+
+def time_serving(G, args, rate):
+    """Poisson arrivals at `rate` requests/s: NFRU from {1250, 2500, 5000,
+    12500}; half paced (cycle length U(400, 2000) ms), half voltage clamp
+    (hold -100 mV, step to U(-40, 40) mV for 200 ms at 5 ms); each request
+    simulates args.serve_ms from rest (a bounded sample of the full protocols),
+    mixed precision, admitted by device bytes."""
+    import numpy as np
+    rng = np.random.default_rng(int(rate * 1000) + 7)
+    n = args.serve_requests
+    srv = G.Server("mixed", slots=args.serve_slots, mem_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
+                   lockstep=args.batch_mode == "lockstep")
+    reqs = []
+    gaps = rng.exponential(1.0 / rate, n)
+    for i in range(n):
+        r = G.Request()
+        r.nfru = int(rng.choice([1250, 2500, 5000, 12500]))
+        if rng.random() < 0.5:
+            r.set = G.settings(period=float(rng.uniform(400.0, 2000.0)))
+        else:
+            r.set = G.settings(vclamp_flag=1, vclamp_hold=-100.0, vclamp_set=float(rng.uniform(-40.0, 40.0)),
+                               vclamp_duration=200.0, vclamp_shift=5.0, vclamp_period=10000.0)
+        r.seed_scheme = G.SEED_BASE
+        r.seed = SEED + 1000003 * i
+        r.pca_scale = 1.0
+        r.duration_ms = float(args.serve_ms)
+        reqs.append(r)
+    t0 = time.perf_counter()
+    nxt = t0
+    for r, g in zip(reqs, gaps):
+        nxt += g
+        d = nxt - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        srv.submit(r)
+    srv.wait()
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = np.array([r.t_done - r.t_submit for r in reqs])
+    wait = np.array([r.t_start - r.t_submit for r in reqs])
+    ok = all(r.status == 0 for r in reqs)
+    cell_ms = n * args.serve_ms
+    eq = sum(r.nfru for r in reqs) / NFRU * args.serve_ms
+    return {"rate_req_per_s": rate, "requests": n, "ok": ok, "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "mean_queue_wait_s": float(wait.mean()),
+            "cell_ms_per_s": cell_ms / wall, "cell_ms_per_s_12500_equiv": eq / wall}
+
+
 def run_gpu(args, dist):
     import numpy as np
     import greenstein2002_gb300 as G
@@ -222,81 +414,39 @@ def run_gpu(args, dist):
     gb.build()
     G.load()
     seed = SEED + dist.rank * args.nfru  # replicas: independent streams per rank
-    # ---- device-resident run (value) ----
-    cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, args.precision)
-    t = 0.0
-    oldstep = st.step_max
-    for _ in range(args.warmup):
-        t, _, _, _ = cell.run(state, t, int(args.step_ms), oldstep, st, want=())
-        oldstep = cell.oldstep
-    sub0 = cell.substeps()
-    launch0 = cell.launches()
-    cell.profile(True)
     clocks = Clocks(dist.local)
-    total_ms = 0.0
-    dist.barrier()
-    cell.sync()
-    clocks.start()
-    for _ in range(args.steps):
-        cell.l2_flush()
-        cell.event(0)
-        t, _, _, _ = cell.run(state, t, int(args.step_ms), oldstep, st, want=())
-        oldstep = cell.oldstep
-        cell.event(1)
-        total_ms += cell.elapsed_ms(0, 1)
-    cell.sync()
-    clk = clocks.stop()
-    dist.barrier()
-    kern_ms, kern_launches = cell.profile_read()
-    cell.profile(False)
-    substeps = cell.substeps() - sub0
-    launches = cell.launches() - launch0 - 0
-    wall_ms = dist.max(total_ms)
-    cells_ms = dist.sum(args.steps * args.step_ms)
-    value = cells_ms / (wall_ms / 1000.0)
-    # roofline of the FRU stage kernel (FP64-pipe bound), measured FP64 peak
+    main = time_single(G, args, dist, args.precision, seed, keep_trace=True, clocks=clocks)
+    wall_ms, substeps = main["wall_ms"], main["substeps"]
+    # roofline of the dominant kernel (the FRU stage kernel), FP64-pipe bound;
+    # the FP64 peak is measured in this run
     fp64_peak = G.fp64_peak_tflops()
-    per_launch_ms = kern_ms / max(kern_launches, 1)
-    sub_per_launch = substeps / max(kern_launches, 1)
+    per_launch_ms = main["kern_ms"] / max(main["kern_launches"], 1)
+    sub_per_launch = substeps / max(main["kern_launches"], 1)
     achieved_tf = FLOPS_PER_SUBSTEP * sub_per_launch / (per_launch_ms * 1e-3) / 1e12
     achieved_gbs = BYTES_PER_SUBSTEP * sub_per_launch / (per_launch_ms * 1e-3) / 1e9
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    cell.close()
+    hbm_peak = load_peaks().get("hbm_gbs", 6800.0)
 
-    # ---- end to end through the C-ABI with host buffers (e2e) ----
-    e2e = None
-    if not args.no_e2e:
-        cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, args.precision)
-        t = 0.0
-        oldstep = st.step_max
-        for _ in range(args.warmup):
-            t, _, _, _ = cell.run(state, t, int(args.step_ms), oldstep, st, want=())
-            oldstep = cell.oldstep
-        host = cell.download()
-        h_state = state.copy()
-        h2d = sum(v.nbytes for v in host.values()) + h_state.nbytes
-        dist.barrier()
-        cell.sync()
-        e2e_ms = 0.0
-        d2h = 0
-        for _ in range(args.steps):
-            cell.l2_flush()
-            t0 = time.perf_counter()
-            cell.upload(host)
-            t, states, other, cur = cell.run(h_state, t, int(args.step_ms), oldstep, st)
-            oldstep = cell.oldstep
-            host = cell.download()
-            e2e_ms += (time.perf_counter() - t0) * 1000.0
-            d2h = sum(v.nbytes for v in host.values()) + states.nbytes + other.nbytes + cur.nbytes
-        dist.barrier()
-        e2e_val = dist.sum(args.steps * args.step_ms) / (dist.max(e2e_ms) / 1000.0)
-        e2e = {"value": e2e_val, "unit": "cell-ms/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
-        cell.close()
+    mixed = None
+    if args.precision == "fp64" and not args.no_mixed:
+        m = time_single(G, args, dist, "mixed", seed, keep_trace=True)
+        a, b = main["trace"], m["trace"]
+        cai_range = float(np.max(a[:, 6]) - np.min(a[:, 6])) or 1.0
+        mixed = {"value": m["value"], "unit": "cell-ms/s", "speedup_vs_fp64": m["value"] / main["value"],
+                 "fru_substeps_per_s": m["substeps"] / (m["wall_ms"] / 1000.0),
+                 "error_vs_fp64_same_seeds": {
+                     "max_abs_dV_mV": float(np.max(np.abs(a[:, 0] - b[:, 0]))),
+                     "max_abs_dCai_rel_to_range": float(np.max(np.abs(a[:, 6] - b[:, 6]))) / cai_range,
+                     "max_rel_dCaNSR": float(np.max(np.abs(a[:, 7] - b[:, 7]) / np.abs(a[:, 7]))),
+                     "window": "per-ms global states over the timed window"}}
+    batched = None if args.no_batch else time_batched(G, args, dist)
+    serving = None
+    if not args.no_serve and dist.world == 1:
+        serving = {"protocol": "per request: %g ms from rest, NFRU in {1250,2500,5000,12500}, 50/50 pacing "
+                               "(CL U(400,2000) ms) or voltage clamp (-100 -> U(-40,40) mV), mixed precision, "
+                               "%d worker slots, %g GB admission budget" % (args.serve_ms, args.serve_slots,
+                                                                            args.serve_budget_gb),
+                   "sweep": [time_serving(G, args, r) for r in args.serve_rates]}
+    e2e = None if args.no_e2e else time_e2e(G, args, dist, seed)
 
     # ---- CPU baseline: the reference program on one host core ----
     cpu = None
@@ -306,14 +456,16 @@ def run_gpu(args, dist):
             v, wall = reference_sample(d, 1, 3.0, SEED)
             cpu = {"value": v, "unit": "cell-ms/s", "cores": 1, "kind": "reference",
                    "sample": "reference program (serial build of its own sources), NFRU=12,500, rest state, "
-                             "first 3 ms (%.1f s wall); rest costs fewer substeps per ms than the paced-beat "
-                             "average timed on the GPU" % wall}
+                             "first 3 ms (%.1f s wall); rest costs fewer substeps per ms than the plateau "
+                             "window timed on the GPU" % wall}
         else:
             cpu = {"value": None, "unit": "cell-ms/s", "cores": 0, "kind": "reference", "sample": why}
 
     if dist.rank == 0:
+        kernel = ("fru_stage_mixed_kernel" if args.precision == "mixed" else
+                  "fru_stage4_kernel" if args.fru_lanes == 4 else "fru_stage_kernel")
         line = {
-            "metric": "cell-ms simulated/s at 12,500 FRUs", "value": value, "unit": "cell-ms/s",
+            "metric": "cell-ms simulated/s at 12,500 FRUs", "value": main["value"], "unit": "cell-ms/s",
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": wall_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
@@ -321,24 +473,28 @@ def run_gpu(args, dist):
                                    "seeds 5489+j; step = %g ms simulated; timed window [%g, %g) ms"
                                    % (args.nfru, args.step_ms, args.warmup * args.step_ms,
                                       (args.warmup + args.steps) * args.step_ms),
-                       "nfru": args.nfru, "step_ms": args.step_ms, "precision": ("fp64 (FRU path and global ODE)" if args.precision == "fp64" else
-                                     "mixed (FRU rates and local Ca ODE fp32; FRU state, clock, flux sums and global ODE fp64)"),
+                       "nfru": args.nfru, "step_ms": args.step_ms,
+                       "precision": ("fp64 (FRU path and global ODE)" if args.precision == "fp64" else
+                                     "mixed (FRU rates and local Ca ODE fp32; FRU state, clock, flux sums "
+                                     "and global ODE fp64)"),
                        "integrator": "host Dormand-Prince 5(4), FRU stages on GPU",
                        "fru_lanes": args.fru_lanes,
                        "l2": "flushed between timed steps (512 MB write)",
                        "parallelism": "replicas" if dist.world > 1 else "single GPU"},
             "fru_substeps": int(substeps), "fru_substeps_per_s": substeps / (wall_ms / 1000.0),
-            "gpu_launches": int(launches),
-            "roofline": {"bound": "fp64", "kernel": ("fru_stage_mixed_kernel" if args.precision == "mixed" else
-                                                     "fru_stage4_kernel" if args.fru_lanes == 4 else "fru_stage_kernel"), "achieved": achieved_tf,
+            "gpu_launches": int(main["launches"]),
+            "roofline": {"bound": "fp64", "kernel": kernel, "achieved": achieved_tf,
                          "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak if fp64_peak else None,
                          "peak_source": "measured in-run (independent DFMA chains on all SMs)",
-                         "traffic": None, "per_launch_ms": per_launch_ms, "launches": int(kern_launches),
+                         "traffic": None, "per_launch_ms": per_launch_ms, "launches": int(main["kern_launches"]),
                          "algorithmic": "%g FLOP x %.0f FRU-substeps per launch" % (FLOPS_PER_SUBSTEP, sub_per_launch),
                          "hbm_view": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                                       "frac": achieved_gbs / hbm_peak,
                                       "algorithmic": "%g B x FRU-substeps" % BYTES_PER_SUBSTEP}},
-            "clocks": clk,
+            "clocks": main["clocks"],
+            "mixed": mixed,
+            "batched": batched,
+            "serving": serving,
             "e2e": e2e,
             "cpu_baseline": cpu,
         }

@@ -52,6 +52,14 @@ class Settings(C.Structure):
             "chfsc_IK1", "chfsc_Jup", "chfsc_INaCa", "chfsc_IKv43", "scale_PCa", "scale_GKr")]
 
 
+class Request(C.Structure):
+    """gw_request of gw_fru.h: one cell simulation submitted to a Server."""
+    _fields_ = [("nfru", C.c_int), ("set", Settings), ("seed_scheme", C.c_int), ("seed", C.c_uint32),
+                ("pca_scale", C.c_double), ("duration_ms", C.c_double), ("v_trace", C.c_void_p),
+                ("final_state", C.c_void_p), ("t_submit", C.c_double), ("t_start", C.c_double),
+                ("t_done", C.c_double), ("status", C.c_int)]
+
+
 _lib = None
 
 
@@ -99,6 +107,18 @@ def bind(path):
         "gw_run": ([vp, P(Settings), P(C.c_double), _dp, P(C.c_double), C.c_int, vp, vp, vp], C.c_int),
         "gw_init_rest": ([vp, P(Settings), C.c_int, C.c_uint32, _dp], C.c_int),
         "gw_dropin_configure": ([C.c_int, C.c_double], None),
+        "gw_batch_create": ([P(vp), C.c_int], C.c_int),
+        "gw_batch_destroy": ([vp], C.c_int),
+        "gw_batch_add": ([vp, vp], C.c_int),
+        "gw_batch_remove": ([vp, vp], C.c_int),
+        "gw_batch_profile": ([vp, C.c_int, P(C.c_double), P(C.c_ulonglong)], C.c_int),
+        "gw_batch_run": ([vp, C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp], C.c_int),
+        "gw_cell_bytes": ([C.c_int], C.c_size_t),
+        "gw_server_create": ([P(vp), C.c_int, C.c_int, C.c_size_t, C.c_int], C.c_int),
+        "gw_run_concurrent": ([C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp], C.c_int),
+        "gw_server_submit": ([vp, P(Request)], C.c_int),
+        "gw_server_wait": ([vp], C.c_int),
+        "gw_server_destroy": ([vp], C.c_int),
         "gw_event_record": ([vp, C.c_int], C.c_int),
         "gw_event_elapsed": ([vp, C.c_int, C.c_int, P(C.c_float)], C.c_int),
         "gw_profile": ([vp, C.c_int], C.c_int),
@@ -275,3 +295,88 @@ def fp64_peak_tflops():
     v = C.c_double(0.0)
     _check(load().gw_probe_fp64_peak(C.byref(v)), "gw_probe_fp64_peak")
     return v.value
+
+
+class Batch:
+    """A gw_batch: many cells advanced by one stage launch per round."""
+
+    def __init__(self, precision="fp64", lib=None):
+        self._L = lib if lib is not None else load()
+        self._h = C.c_void_p()
+        _check(self._L.gw_batch_create(C.byref(self._h), 1 if precision in (1, "mixed") else 0), "gw_batch_create",
+               self._L)
+
+    def close(self):
+        if self._h:
+            self._L.gw_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def profile(self, enable=True):
+        ms, n = C.c_double(0.0), C.c_ulonglong(0)
+        _check(self._L.gw_batch_profile(self._h, 1 if enable else 0, C.byref(ms), C.byref(n)), "gw_batch_profile",
+               self._L)
+        return ms.value, n.value
+
+    def run(self, cells, sets, t, states, oldsteps, n_steps, traces=False, lockstep=True):
+        """Advance every cell n_steps output steps concurrently (one host thread
+        per cell); t, states (n, 37) and oldsteps advance in place.  With
+        traces=True returns per-step states (n, n_steps, 37) and otherstates
+        (n, n_steps, 12)."""
+        n = len(cells)
+        st_tr = np.zeros((n, n_steps, NSTATE)) if traces else None
+        ot_tr = np.zeros((n, n_steps, NOTHER)) if traces else None
+        handles = (C.c_void_p * n)(*[c._h.value for c in cells])
+        setarr = (Settings * n)(*sets)
+        for a in (t, states, oldsteps):
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+        args = (C.cast(setarr, C.c_void_p), t.ctypes.data_as(C.c_void_p), states.ctypes.data_as(C.c_void_p),
+                oldsteps.ctypes.data_as(C.c_void_p), int(n_steps), _ptr(st_tr), _ptr(ot_tr))
+        if lockstep:
+            _check(self._L.gw_batch_run(self._h, n, handles, *args), "gw_batch_run", self._L)
+        else:
+            _check(self._L.gw_run_concurrent(n, handles, *args), "gw_run_concurrent", self._L)
+        return (st_tr, ot_tr) if traces else None
+
+
+class Server:
+    """A gw_server: requests run concurrently through one batch (continuous
+    batching), admitted by device bytes."""
+
+    def __init__(self, precision="mixed", slots=32, mem_budget_bytes=64 << 30, lockstep=False, lib=None):
+        self._L = lib if lib is not None else load()
+        self._h = C.c_void_p()
+        _check(self._L.gw_server_create(C.byref(self._h), 1 if precision in (1, "mixed") else 0, int(slots),
+                                        int(mem_budget_bytes), 1 if lockstep else 0), "gw_server_create", self._L)
+        self._keep = []
+
+    def submit(self, req, v_trace=None, final_state=None):
+        if v_trace is not None:
+            req.v_trace = v_trace.ctypes.data_as(C.c_void_p)
+        if final_state is not None:
+            req.final_state = final_state.ctypes.data_as(C.c_void_p)
+        self._keep.append((req, v_trace, final_state))
+        _check(self._L.gw_server_submit(self._h, C.byref(req)), "gw_server_submit", self._L)
+
+    def wait(self):
+        _check(self._L.gw_server_wait(self._h), "gw_server_wait", self._L)
+
+    def close(self):
+        if self._h:
+            self._L.gw_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cell_bytes(nfru):
+    return int(load().gw_cell_bytes(int(nfru)))

@@ -25,6 +25,8 @@ CUDA_UNITS = {
     "gw_fru_stage.cu": ["-fmad=false"],
     "gw_fru_stage4.cu": ["-fmad=false"],
     "gw_fru_mixed.cu": [],
+    "gw_batch.cu": [],
+    "gw_serve.cu": [],
     "gw_abi.cu": [],
     "gw_probe.cu": [],
     "gw_noalloc.cu": ["-fmad=false"],
@@ -81,7 +83,7 @@ def build(force=False, verbose=False):
         for out in ex.map(run, jobs):
             if verbose and out.strip():
                 print(out)
-    run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lm"])
+    run([nvcc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lm", "-lpthread"])
     # the C host driver (caf.c main loop) linked against the library
     run([cc, "-O2", "-std=c99", "-ffp-contract=off", "-Wall", "-I" + CSRC, "-I" + INC, "-o", EXE,
          os.path.join(HERE, "host", "gw_caf.c"), "-L" + OUT, "-lgw_fru", "-Wl,-rpath,$ORIGIN", "-lm"])

@@ -14,6 +14,7 @@
 #include "gw_fru.h"
 #include "gw_kernels.h"
 #include "gw_fru_model.cuh"
+#include "gw_ctx_impl.h"
 
 using gw::DevState;
 using gw::StageParams;
@@ -34,25 +35,6 @@ static int set_err(int code, const char* fmt, ...) {
     if (e_ != cudaSuccess) return set_err(GW_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
                                           __FILE__, __LINE__);                                  \
   } while (0)
-
-struct gw_ctx {
-  DevState d;
-  cudaStream_t stream = nullptr;
-  double* h_out = nullptr;  // pinned [32]
-  double nfru_scale = 1.0;
-  uint32_t epoch = 0;
-  int pending = 0;          // kFlagSave / kFlagResume to fold into the next launch
-  int device = 0;
-  cudaEvent_t ev[8] = {};
-  cudaEvent_t pev[2] = {};  // bracket of the last stage launch while profiling
-  bool profiling = false;
-  double prof_ms = 0.0;
-  unsigned long long prof_launches = 0, launches = 0;
-  void* flush_buf = nullptr;
-  int fru_lanes = 4;        // lanes per FRU of the stage kernel: 1 or 4
-  int precision = 0;        // 0: FP64, 1: mixed (FP32 rates and local ODE)
-  double pca_scale = 1.0;   // LCC permeability scale of the cell
-};
 
 static cudaError_t launch_stage_variant(gw_ctx* c, const StageParams& p) {
   if (c->precision == 1) return gw::launch_stage_mixed(c->d, p, c->stream);
@@ -231,6 +213,10 @@ static int flush_pending(gw_ctx* c) {
   p.nfru_scale = c->nfru_scale;
   p.pca_scale = c->pca_scale;
   c->pending = 0;
+  if (c->batch) {
+    double out[32];
+    return gw_batch_post(c, p, out);
+  }
   CK(launch_stage_variant(c, p));
   c->launches++;
   return GW_OK;
@@ -292,6 +278,18 @@ static int run_stage(gw_ctx* c, double t0, double tf, const double dep0[3], cons
   p.epoch = c->epoch;
   p.flags = c->pending | (advance ? gw::kFlagAdvance : 0);
   c->pending = 0;
+  if (c->batch) {
+    int rc = gw_batch_post(c, p, c->h_out);
+    if (rc) return rc;
+    if (c->h_out[gw::kOutError] != 0.0)
+      return set_err(GW_EINVAL, "FRU stage [%g, %g]: substep limit reached (corrupted FRU state: NaN or "
+                     "out-of-range concentrations)", t0, tf);
+    if (num)
+      for (int k = 0; k < 5; k++) num[k] = c->h_out[k];
+    if (out)
+      for (int k = 0; k < 4; k++) out[k] = c->h_out[5 + k];
+    return GW_OK;
+  }
   if (c->profiling) CK(cudaEventRecord(c->pev[0], c->stream));
   CK(launch_stage_variant(c, p));
   c->launches++;

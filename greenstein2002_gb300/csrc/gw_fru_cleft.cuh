@@ -483,18 +483,49 @@ __device__ __forceinline__ void advance4(const StageCtx& sc, const Group& g, dou
   }
 }
 
-// The stage kernel: load, optional snapshot save/restore, advance, store,
-// and the fused deterministic flux reduction (calc_fru_flux_local.c:28-77,
-// mpi_master.c:447-468, mpi_slave.c:150-226).
+// Last-block pass of one cell whose blocks are bidx = 0..nblocks-1 of a
+// (possibly multi-cell) grid: partial sums in fixed block order.
+template <int NV>
+__device__ __forceinline__ bool cell_finish(const double v[NV], double* partials, unsigned* ticket, double* smem,
+                                            double tot[NV], int bidx, int nblocks) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) partials[bidx * NV + k] = v[k];
+    __threadfence();
+    last = (atomicAdd(ticket, 1u) == (unsigned)nblocks - 1u);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double s[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) s[k] = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < NV; k++) s[k] += __ldcg(&partials[b * NV + k]);
+  block_reduce<NV>(s, smem);
+  if (threadIdx.x == 0) {
+    *ticket = 0u;
+#pragma unroll
+    for (int k = 0; k < NV; k++) tot[k] = s[k];
+  }
+  return threadIdx.x == 0;
+}
+
+// The stage of one cell, block bidx of its nblocks: load, optional snapshot
+// save/restore, advance, store, and the fused deterministic flux reduction
+// (calc_fru_flux_local.c:28-77, mpi_master.c:447-468, mpi_slave.c:150-226);
+// the cell's totals go to out[0..8] and its error flag to out[kOutError].
 template <typename R>
-__device__ __forceinline__ void stage_body(DevState& s, const StageParams& p) {
+__device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, int bidx, int nblocks, double* out) {
   __shared__ double smem[32 * 5];
   const int lane = threadIdx.x & 31;
   Group g;
   g.c = lane & 3;
   g.base = lane & ~3;
   g.mask = 0xfu << g.base;
-  const int f = blockIdx.x * 8 + (threadIdx.x >> 2);
+  const int f = bidx * 8 + (threadIdx.x >> 2);
   double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   uint32_t nsub = 0;
   bool overflow = false;
@@ -545,7 +576,7 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p) {
     if (cl_of(w) == 2) v[4] = 1.0;
   }
   __syncwarp();
-  if (overflow) s.out[kOutError] = 1.0;
+  if (overflow) out[kOutError] = 1.0;
   if (s.substeps) {
     unsigned long long c = (g.c == 0) ? nsub : 0;
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
@@ -553,15 +584,34 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p) {
   }
   block_reduce<5>(v, smem);
   double tot[5];
-  if (grid_finish<5>(v, s.partials, s.ticket, smem, tot)) {
+  if (cell_finish<5>(v, s.partials, s.ticket, smem, tot, bidx, nblocks)) {
     double cur[4];
     currents_from_sums(s.nfru, p.nfru_scale, p.depf, tot, cur);
     cur[2] = cur[2] * p.pca_scale;  // ICa is proportional to the LCC permeability
 #pragma unroll
-    for (int k2 = 0; k2 < 5; k2++) s.out[k2] = tot[k2];
+    for (int k2 = 0; k2 < 5; k2++) out[k2] = tot[k2];
 #pragma unroll
-    for (int k2 = 0; k2 < 4; k2++) s.out[5 + k2] = cur[k2];
+    for (int k2 = 0; k2 < 4; k2++) out[5 + k2] = cur[k2];
   }
+}
+
+// ---- many cells in one launch ------------------------------------------------
+// Cell i owns blocks block0[i] .. block0[i+1]-1 of the grid (8 FRUs each);
+// its parameters are params[i] and its totals go to outs[i*32 ..].
+template <typename R>
+__device__ __forceinline__ void batch_body(const BatchArgs& a) {
+  // the cell of this block: binary search of the block prefix sums
+  int lo = 0, hi = a.ncells - 1;
+  const int b = blockIdx.x;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&a.block0[mid]) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  DevState s = a.cells[lo];
+  const StageParams p = a.params[lo];
+  if (p.flags < 0) return;  // the cell posted no operation this round
+  stage_body<R>(s, p, b - a.block0[lo], a.block0[lo + 1] - a.block0[lo], a.outs + kBatchOutStride * lo);
 }
 
 }  // namespace cleft

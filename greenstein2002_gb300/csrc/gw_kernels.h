@@ -54,7 +54,22 @@ struct StageParams {
   int flags;
 };
 
+// Many cells in one launch (cleft-parallel kernels): cell i owns blocks
+// block0[i] .. block0[i+1]-1 (8 FRUs per block); params[i].flags < 0 means
+// the cell has no operation this round; its totals go to outs[i*32 ..] in the
+// layout of DevState::out.
+constexpr int kBatchOutStride = 32;
+struct BatchArgs {
+  const DevState* cells;
+  const StageParams* params;
+  const int* block0;  // ncells + 1 prefix sums
+  double* outs;       // [ncells][kBatchOutStride]
+  int ncells;
+};
+
 cudaError_t launch_stage(const DevState& s, const StageParams& p, cudaStream_t st);
+cudaError_t launch_stage4_batch(const BatchArgs& a, int nblocks, cudaStream_t st);
+cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, cudaStream_t st);
 // cleft-parallel variants: 4 lanes per FRU, 8 FRUs per single-warp block;
 // FP64 (the plain method) and mixed precision (FP32 rates and local ODE)
 cudaError_t launch_stage4(const DevState& s, const StageParams& p, cudaStream_t st);

@@ -21,6 +21,7 @@
 #ifndef GW_FRU_H
 #define GW_FRU_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -168,6 +169,63 @@ int gw_run(gw_ctx *ctx, const gw_settings *set, double *t, double *state, double
  * 37 globals (CaTOT from the FRU sums) and every FRU at rest, seeded by
  * `scheme`/`base` as in gw_seed. */
 int gw_init_rest(gw_ctx *ctx, const gw_settings *set, int scheme, uint32_t base, double *state);
+
+/* ------------------------------------------------------------------------- */
+/* Batching: many cells, one stage launch per round (no reference            */
+/* counterpart; the reference runs one cell per MPI job)                      */
+/* ------------------------------------------------------------------------- */
+typedef struct gw_batch gw_batch;
+/* precision as gw_set_precision; member cells must use the same precision and
+ * the default 4-lane kernel. */
+int gw_batch_create(gw_batch **batch, int precision);
+int gw_batch_destroy(gw_batch *batch);
+/* Join / leave between rounds.  While a member, a cell's stage and flux
+ * operations wait for the round in which every member has posted one; each
+ * member must therefore be driven by its own host thread.  A cell's results
+ * do not depend on which other cells share its rounds. */
+int gw_batch_add(gw_batch *batch, gw_ctx *ctx);
+int gw_batch_remove(gw_batch *batch, gw_ctx *ctx);
+/* Batched-kernel device time and launches since the last call (enable != 0
+ * starts measuring). */
+int gw_batch_profile(gw_batch *batch, int enable, double *kernel_ms, unsigned long long *launches);
+/* Run n cells for n_steps output steps each, one host thread per cell:
+ * states[n][37], t[n], oldsteps[n] advance in place; state_trace
+ * [n][n_steps][37] and other_trace [n][n_steps][12] (either may be NULL)
+ * receive every output step's states and otherstates. */
+int gw_batch_run(gw_batch *batch, int n, gw_ctx **cells, const gw_settings *sets, double *t, double *states,
+                 double *oldsteps, int n_steps, double *state_trace, double *other_trace);
+/* The same without shared rounds: each cell on its own stream and host
+ * thread, its kernels running concurrently with the others'. */
+int gw_run_concurrent(int n, gw_ctx **cells, const gw_settings *sets, double *t, double *states, double *oldsteps,
+                      int n_steps, double *state_trace, double *other_trace);
+
+/* ------------------------------------------------------------------------- */
+/* Serving: requests arrive at any time and run concurrently through one     */
+/* batch (continuous batching; no reference counterpart)                      */
+/* ------------------------------------------------------------------------- */
+typedef struct gw_request {
+  int nfru;                /* FRUs of the cell */
+  gw_settings set;         /* protocol (pacing or voltage clamp) and conductance scales */
+  int seed_scheme;         /* as gw_seed */
+  uint32_t seed;
+  double pca_scale;        /* LCC permeability scale (0 or 1: the reference) */
+  double duration_ms;      /* simulated time from the rest state */
+  double *v_trace;         /* optional host buffer: V at every output step */
+  double *final_state;     /* optional host buffer [37] */
+  double t_submit, t_start, t_done; /* host clock seconds, set by the server */
+  int status;              /* -1 while pending, then a GW_* status */
+} gw_request;
+typedef struct gw_server gw_server;
+/* Device bytes a cell of nfru FRUs holds (the admission unit). */
+size_t gw_cell_bytes(int nfru);
+/* slots worker threads; requests are admitted in arrival order while their
+ * cells fit in mem_budget_bytes next to the running ones.  lockstep = 1 runs
+ * the admitted cells through one gw_batch; 0 gives each its own stream. */
+int gw_server_create(gw_server **srv, int precision, int slots, size_t mem_budget_bytes, int lockstep);
+/* Non-blocking; req must stay valid until gw_server_wait returns. */
+int gw_server_submit(gw_server *srv, gw_request *req);
+int gw_server_wait(gw_server *srv);
+int gw_server_destroy(gw_server *srv);
 
 /* ------------------------------------------------------------------------- */
 /* Drop-in layer: reference names and signatures (parameters.h:255-271).      */

@@ -1,0 +1,68 @@
+"""Serving (gw_server): requests of different FRU counts and protocols arrive
+while others run, are admitted by device bytes, and share stage launches.
+Each result must be the same alone and in the mix."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _req(gw, nfru, seed, clamp=False, period=1000.0, dur=12.0):
+    r = gw.Request()
+    r.nfru = nfru
+    if clamp:
+        r.set = gw.settings(vclamp_flag=1, vclamp_hold=-100.0, vclamp_set=10.0, vclamp_duration=200.0,
+                            vclamp_shift=5.0, vclamp_period=1000.0)
+    else:
+        r.set = gw.settings(period=period)
+    r.seed_scheme = gw.SEED_BASE
+    r.seed = seed
+    r.pca_scale = 1.0
+    r.duration_ms = dur
+    return r
+
+
+@pytest.mark.parametrize("lockstep", [False, True])
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_result_same_alone_and_in_the_mix(gw, prec, lockstep):
+    dur = 12
+    # alone
+    srv = gw.Server(prec, slots=4, mem_budget_bytes=8 << 30, lockstep=lockstep)
+    a = _req(gw, 500, 77, clamp=False, dur=dur)
+    va, fa = np.zeros(dur), np.zeros(37)
+    srv.submit(a, va, fa)
+    srv.wait()
+    srv.close()
+    assert a.status == 0
+    # in a mix of pacing and clamp requests of other sizes
+    srv = gw.Server(prec, slots=6, mem_budget_bytes=8 << 30, lockstep=lockstep)
+    reqs = [_req(gw, 300, 5, clamp=True, dur=dur), _req(gw, 800, 9, period=400.0, dur=dur),
+            _req(gw, 500, 77, clamp=False, dur=dur), _req(gw, 150, 3, clamp=True, dur=dur)]
+    outs = [(np.zeros(dur), np.zeros(37)) for _ in reqs]
+    for r, (v, f) in zip(reqs, outs):
+        srv.submit(r, v, f)
+    srv.wait()
+    srv.close()
+    assert all(r.status == 0 for r in reqs)
+    np.testing.assert_array_equal(outs[2][0], va)
+    np.testing.assert_array_equal(outs[2][1], fa)
+    # the clamp requests hold V at the clamp levels
+    assert np.all(np.abs(outs[0][0][:3] + 100.0) < 1e-9) and abs(outs[0][0][-1] - 10.0) < 1e-9
+
+
+def test_admission_by_device_bytes(gw):
+    # a budget that fits two 1000-FRU cells: never more than two run at once
+    budget = 2 * gw.cell_bytes(1000) + 1024
+    srv = gw.Server("mixed", slots=8, mem_budget_bytes=budget)
+    reqs = [_req(gw, 1000, 100 + i, dur=4) for i in range(6)]
+    for r in reqs:
+        srv.submit(r)
+    srv.wait()
+    srv.close()
+    assert all(r.status == 0 for r in reqs)
+    ev = sorted([(r.t_start, 1) for r in reqs] + [(r.t_done, -1) for r in reqs])
+    live = peak = 0
+    for _, d in ev:
+        live += d
+        peak = max(peak, live)
+    assert peak <= 2
