@@ -254,6 +254,38 @@ extern "C" int gw_download(gw_ctx* c, double* frus, int* ltype, int* ryr, int* i
   return GW_OK;
 }
 
+extern "C" int gw_download_range(gw_ctx* c, int first, int count, double* frus, int* ltype, int* ryr, int* ito2) {
+  if (!c) return set_err(GW_EINVAL, "gw_download_range: null context");
+  if (first < 0 || count <= 0 || first + count > c->d.nfru)
+    return set_err(GW_EINVAL, "gw_download_range: FRUs %d..%d outside 0..%d", first, first + count - 1,
+                   c->d.nfru - 1);
+  int rc = flush_pending(c);
+  if (rc) return rc;
+  const size_t nf = (size_t)c->d.stride;
+  std::vector<double> hf(5 * (size_t)count);
+  std::vector<uint32_t> hc(4 * (size_t)count);
+  CK(cudaMemcpy2DAsync(hf.data(), count * sizeof(double), c->d.frus + first, nf * sizeof(double),
+                       count * sizeof(double), 5, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpy2DAsync(hc.data(), count * sizeof(uint32_t), c->d.chan + first, nf * sizeof(uint32_t),
+                       count * sizeof(uint32_t), 4, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int f = 0; f < count; f++) {
+    if (frus)
+      for (int i = 0; i < 5; i++) frus[5 * f + i] = hf[(size_t)i * count + f];
+    for (int k = 0; k < 4; k++) {
+      const uint32_t w = hc[(size_t)k * count + f];
+      if (ltype) {
+        ltype[8 * f + 2 * k] = (int)(w & 15u);
+        ltype[8 * f + 2 * k + 1] = (int)((w >> 4) & 15u);
+      }
+      if (ryr)
+        for (int i = 0; i < 5; i++) ryr[20 * f + 5 * k + i] = (int)((w >> (8 + 4 * i)) & 15u);
+      if (ito2) ito2[4 * f + k] = (int)(w >> 28);
+    }
+  }
+  return GW_OK;
+}
+
 extern "C" int gw_seed(gw_ctx* c, int scheme, uint32_t base) {
   if (!c || (scheme != gw::kSeedBase && scheme != gw::kSeedReference))
     return set_err(GW_EINVAL, "gw_seed: bad context or scheme %d", scheme);

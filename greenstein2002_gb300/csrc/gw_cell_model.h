@@ -73,6 +73,15 @@ typedef gw_settings gw_protocol;
 #define GWC_KBSR 0.00087
 #define GWC_BSLtot 1.124
 #define GWC_KBSL 0.0087
+/* FRU flux constants used by the per-FRU property output
+ * (parameters_fcn_fru.c:24-25, :48-50, :83-87) */
+#define GWC_Clo 150.0
+#define GWC_Cli 20.0
+#define GWC_PCa (1.5 / 2.8 * 0.2 * 0.9 * 0.9468e-11)
+#define GWC_PCl 2.65e-15
+#define GWC_JRyRmax (0.6 * 1.5 * 1.1 * 3.96)
+#define GWC_tautr 3.0
+#define GWC_tauxfer 0.005
 
 GW_HD void gw_protocol_defaults(gw_protocol* p) {
   /* parameters.h:92-156 */

@@ -14,8 +14,10 @@
  * Inputs and outputs keep the reference's formats byte for byte:
  * ic/stable/ic_*.txt (initialize_state.c:43-163, rewound every
  * min(NFRU,1250) FRUs), states.N.txt / otherstates.N.txt / currents.N.txt
- * (data_io.c:22-140), and the r_*.N.txt checkpoint files (data_io.c:197-268)
- * every Ndump output steps.
+ * (data_io.c:22-140), the r_*.N.txt checkpoint files (data_io.c:197-268)
+ * every Ndump output steps, and with write_fru_props_flag = 1 the per-FRU
+ * property files fruprops_J.N.txt, fruprops_avg_J.N.txt and
+ * fruprops_avg_tot.N.txt for FRUs fru_start..fru_end (write_fru_props.c).
  */
 #include <ctype.h>
 #include <math.h>
@@ -30,6 +32,7 @@
 typedef struct {
     gw_settings s;
     int nfru, ts_sec, ic_file_flag, Ndump, filenumber0, seed_scheme;
+    int write_fru_props_flag, fru_start, fru_end, fru_props_compat;
     unsigned long seed_base;
     char ic_dir[512], output_dir[512];
     char ic_states[128], ic_FRU[128], ic_LCh[128], ic_RyR[128], ic_Ito2[128];
@@ -46,6 +49,8 @@ static void cfg_defaults(run_cfg *c)
     c->filenumber0 = 0;
     c->seed_scheme = 1;        /* the reference's initialize_ran.c formula */
     c->seed_base = 5489;
+    c->fru_start = 0;          /* parameters.h:203-205 */
+    c->fru_end = 9;
     strcpy(c->ic_dir, "ic/stable");
     strcpy(c->output_dir, "./");
     strcpy(c->ic_states, "ic_states_stable.txt");
@@ -89,6 +94,10 @@ static int set_key(run_cfg *c, const char *k, const char *v)
     if (!strcmp(k, "filenumber0")) { c->filenumber0 = atoi(v); return 0; }
     if (!strcmp(k, "seed_scheme")) { c->seed_scheme = atoi(v); return 0; }
     if (!strcmp(k, "seed_base")) { c->seed_base = strtoul(v, NULL, 10); return 0; }
+    if (!strcmp(k, "write_fru_props_flag")) { c->write_fru_props_flag = atoi(v); return 0; }
+    if (!strcmp(k, "fru_start")) { c->fru_start = atoi(v); return 0; }
+    if (!strcmp(k, "fru_end")) { c->fru_end = atoi(v); return 0; }
+    if (!strcmp(k, "fru_props_compat")) { c->fru_props_compat = atoi(v); return 0; }
 #define STR(field, name) if (!strcmp(k, name)) { snprintf(c->field, sizeof c->field, "%s", v); return 0; }
     STR(ic_dir, "ic_dir") STR(output_dir, "output_dir") STR(ic_states, "ic_states_file") STR(ic_FRU, "ic_FRU_file")
     STR(ic_LCh, "ic_LCh_file") STR(ic_RyR, "ic_RyR_file") STR(ic_Ito2, "ic_Ito2_file")
@@ -286,6 +295,120 @@ static void restart_data(const run_cfg *c, int num, const double *state, gw_ctx 
     free(frus); free(ltype); free(ryr); free(ito2);
 }
 
+/* ---- per-FRU property files (write_fru_props.c:28-188) ------------------- */
+typedef struct {
+    FILE **fru, **avg, *tot;
+    int n;                     /* fru_end - fru_start + 1 */
+    double *frus;
+    int *ltype, *ryr, *ito2;
+} fru_props;
+
+static void open_props(const run_cfg *c, int num, fru_props *p)
+{
+    char stem[64];
+    int j;
+    for (j = 0; j < p->n; j++) {
+        snprintf(stem, sizeof stem, "fruprops_%d", c->fru_start + j);
+        p->fru[j] = open_out(c, stem, num);
+        fprintf(p->fru[j], "%s %s %s %s %s %s %s %s %s\n", "Time", "JLType", "JRyR", "Jtr", "Jxfer", "CaSS", "CaJSR",
+                "Ito2", "NRyR_open");
+    }
+    for (j = 0; j < p->n; j++) {
+        snprintf(stem, sizeof stem, "fruprops_avg_%d", c->fru_start + j);
+        p->avg[j] = open_out(c, stem, num);
+        fprintf(p->avg[j], "%s %s %s %s %s %s %s %s %s\n", "Time", "JLType_tot", "JRyR_tot", "Jtr", "Jxfer_tot",
+                "CaSS_avg", "CaJSR", "Ito2", "PRyR_open");
+    }
+    p->tot = open_out(c, "fruprops_avg_tot", num);
+    fprintf(p->tot, "%s %s %s %s %s %s %s %s %s\n", "Time", "JLType_totAll", "JRyR_totAll", "Jtr_totAll",
+            "Jxfer_totAll", "CaSS_avgAll", "CaJSR_avgAll", "Ito2", "PRyR_openAll");
+}
+
+static void close_props(fru_props *p)
+{
+    int j;
+    for (j = 0; j < p->n; j++) {
+        fclose(p->fru[j]);
+        fclose(p->avg[j]);
+    }
+    fclose(p->tot);
+}
+
+/* One output step of write_fru_props.c:28-128: only the selected FRUs are
+ * read back from the device.  The reference tests an FRU's LCC as
+ * LType_state[j][index_LCC_states][jcleft] and its voltage gate as
+ * LType_state[j][index_LCC_Vinact][jcleft] (write_fru_props.c:90-91), with
+ * the cleft and state subscripts swapped; this writes the LCC flux of the
+ * cleft's own channel, or with fru_props_compat = 1 reads the same words of
+ * the FRU's row as that code does (row offsets jcleft and 2 + jcleft). */
+static void write_props(const run_cfg *c, fru_props *p, gw_ctx *ctx, double time, const double *state)
+{
+    const double V = state[GW_V], Cai = state[GW_Cai], CaNSR = state[GW_CaNSR];
+    const double tprint = c->ts_sec ? time * 1.e-3 : time;
+    const double VF_over_RT = V / GWC_RT_over_F, VFsq_over_RT = (1000.0 * GWC_Faraday) * VF_over_RT;
+    const double pca = GWC_PCa * c->s.scale_PCa;
+    double JLType_totALL = 0.0, JRyR_totALL = 0.0, Jtr_totALL = 0.0, Jxfer_totALL = 0.0;
+    double CaSS_avgALL = 0.0, CaJSR_avgALL = 0.0, PRyR_openALL = 0.0, Ito2_avgALL = 0.0, num_avg;
+    int j, q, i;
+    if (gw_download_range(ctx, c->fru_start, p->n, p->frus, p->ltype, p->ryr, p->ito2)) {
+        fprintf(stderr, "write_fru_props: download failed: %s\n", gw_last_error());
+        exit(4);
+    }
+    for (j = 0; j < p->n; j++) {
+        const double CaJSR = p->frus[5 * j];
+        const int *lt = p->ltype + 8 * j;
+        double JLType_tot1 = 0.0, JRyR_tot1 = 0.0, Jxfer_tot1 = 0.0, CaSS_avg1 = 0.0, PRyR_open1 = 0.0;
+        double Ito2_tot1 = 0.0, Jtr;
+        CaJSR_avgALL = CaJSR_avgALL + CaJSR;
+        Jtr = (CaNSR - CaJSR) / GWC_tautr * GWC_VJSR / GWC_Vmyo;
+        Jtr_totALL = Jtr_totALL + Jtr;
+        for (q = 0; q < 4; q++) {
+            const double CaSS = p->frus[5 * j + q + 1];
+            const int lcc = c->fru_props_compat ? lt[q] : lt[2 * q];
+            const int vdi = c->fru_props_compat ? lt[2 + q] : lt[2 * q + 1];
+            double JLType = 0.0, Ito2 = 0.0, JRyR, Jxfer;
+            int nopen = 0;
+            CaSS_avg1 += CaSS;
+            CaSS_avgALL += CaSS;
+            if ((lcc == 6 || lcc == 12) && vdi == 2) { /* O1_LType, O2_LType, Oy_LType */
+                JLType = pca * 4.0 * VFsq_over_RT * (CaSS * exp(2.0 * VF_over_RT) - GWC_Cao * 0.341) /
+                         (exp(2.0 * VF_over_RT) - 1.0) / (-2.0 * GWC_Vmyo * GWC_Faraday * 1000.0);
+                JLType_tot1 += JLType;
+                JLType_totALL += JLType;
+            }
+            if (p->ito2[4 * j + q] == 2) { /* O_Ito2 */
+                Ito2 = GWC_PCl * VFsq_over_RT * (GWC_Cli * exp(-VF_over_RT) - GWC_Clo) / (exp(-VF_over_RT) - 1.0);
+                Ito2_tot1 += Ito2;
+                Ito2_avgALL += Ito2;
+            }
+            for (i = 0; i < 5; i++) {
+                const int r = p->ryr[20 * j + 5 * q + i];
+                if (r == 3 || r == 4 || r == 7) nopen = nopen + 1; /* O1_RyR, O2_RyR, O3_RyR */
+            }
+            PRyR_open1 = PRyR_open1 + (double)nopen;
+            PRyR_openALL = PRyR_openALL + (double)nopen;
+            JRyR = GWC_JRyRmax * (double)nopen * (CaJSR - CaSS) * GWC_VSS / GWC_Vmyo;
+            JRyR_tot1 = JRyR_tot1 + JRyR;
+            JRyR_totALL = JRyR_totALL + JRyR;
+            Jxfer = (CaSS - Cai) / GWC_tauxfer * GWC_VSS / GWC_Vmyo;
+            Jxfer_tot1 = Jxfer_tot1 + Jxfer;
+            Jxfer_totALL = Jxfer_totALL + Jxfer;
+            fprintf(p->fru[j], "%.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %d\n", tprint, JLType, JRyR, Jtr, Jxfer, CaSS,
+                    CaJSR, Ito2, nopen);
+        }
+        CaSS_avg1 = CaSS_avg1 / 4;
+        PRyR_open1 = PRyR_open1 / (double)(5 * 4);
+        fprintf(p->avg[j], "%.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g\n", tprint, JLType_tot1, JRyR_tot1, Jtr,
+                Jxfer_tot1, CaSS_avg1, CaJSR, Ito2_tot1, PRyR_open1);
+    }
+    num_avg = (double)p->n;
+    CaSS_avgALL = CaSS_avgALL / num_avg / 4;
+    CaJSR_avgALL = CaJSR_avgALL / num_avg;
+    PRyR_openALL = PRyR_openALL / (num_avg * (double)(5 * 4));
+    fprintf(p->tot, "%.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g %.8g\n", tprint, JLType_totALL, JRyR_totALL, Jtr_totALL,
+            Jxfer_totALL, CaSS_avgALL, CaJSR_avgALL, Ito2_avgALL, PRyR_openALL);
+}
+
 /* initial conditions (initialize_ran.c + initialize_state.c) */
 static void init_cell(const run_cfg *c, gw_ctx *ctx, double *state)
 {
@@ -330,6 +453,7 @@ int main(int argc, char **argv)
     double time_now, tstep, oldstep, iv_time = 0.0;
     int filenumber, n_restart = 0, a, rc;
     FILE *fst, *fcu, *fot;
+    fru_props props;
     clock_t c0 = clock();
 
     cfg_defaults(&c);
@@ -361,6 +485,29 @@ int main(int argc, char **argv)
     fst = open_states(&c, filenumber);
     fcu = open_currents(&c, filenumber);
     fot = open_otherstates(&c, filenumber);
+    memset(&props, 0, sizeof props);
+    if (c.write_fru_props_flag) {
+        if (c.fru_end >= c.nfru) { /* write_fru_props.c:60-68 */
+            fprintf(stderr, "Inappropriate fru_end (%d) in write_fru_props\n", c.fru_end);
+            exit(-3);
+        }
+        if (c.fru_start < 0 || c.fru_start > c.fru_end) {
+            fprintf(stderr, "Inappropriate fru_start (%d) in write_fru_props\n", c.fru_start);
+            exit(-4);
+        }
+        props.n = c.fru_end - c.fru_start + 1;
+        props.fru = malloc(sizeof(FILE *) * props.n);
+        props.avg = malloc(sizeof(FILE *) * props.n);
+        props.frus = malloc(sizeof(double) * 5 * props.n);
+        props.ltype = malloc(sizeof(int) * 8 * props.n);
+        props.ryr = malloc(sizeof(int) * 20 * props.n);
+        props.ito2 = malloc(sizeof(int) * 4 * props.n);
+        if (!props.fru || !props.avg || !props.frus || !props.ltype || !props.ryr || !props.ito2) {
+            fprintf(stderr, "write_fru_props: out of host memory\n");
+            exit(4);
+        }
+        open_props(&c, filenumber, &props);
+    }
     printf("%s %s %s %s\n", "Time", "Phase", "NFRU", "V");
     for (time_now = c.s.time_start; time_now <= c.s.time_end - .0001 * c.s.time_step; time_now += c.s.time_step) {
         printf("%g %i %i %g\n", time_now, 1, c.nfru, state[GW_V]);
@@ -383,17 +530,21 @@ int main(int argc, char **argv)
         }
         write_row(fst, &c, tstep, state, GW_NSTATE, "%.8g ");
         write_row(fot, &c, tstep, other, GW_NOTHER, "%g ");
+        if (c.write_fru_props_flag) write_props(&c, &props, ctx, tstep, state);
         if (n_restart >= c.Ndump) {
             n_restart = 0;
             restart_data(&c, filenumber, state, ctx);
             filenumber = filenumber + 1;
             fclose(fot);
             fclose(fst);
+            if (c.write_fru_props_flag) close_props(&props);
             if (time_now < c.s.time_end - 1.0001 * c.s.time_step) {
                 fst = open_states(&c, filenumber);
                 fot = open_otherstates(&c, filenumber);
+                if (c.write_fru_props_flag) open_props(&c, filenumber, &props);
             } else {
                 fst = fot = NULL;
+                props.tot = NULL;
             }
         }
         if (c.s.iv_flag && iv_time >= c.s.iv_clamp_period) {
@@ -411,6 +562,7 @@ int main(int argc, char **argv)
     fclose(fcu);
     if (fot) fclose(fot);
     if (fst) fclose(fst);
+    if (c.write_fru_props_flag && props.tot) close_props(&props);
     gw_destroy(ctx);
     printf("Total time: %fs\n", (double)(clock() - c0) / (double)CLOCKS_PER_SEC);
     return 0;

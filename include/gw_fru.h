@@ -60,6 +60,10 @@ int gw_set_scale(gw_ctx *ctx, double nfru_scale);
 int gw_upload(gw_ctx *ctx, const double *frus, const int *ltype, const int *ryr, const int *ito2, const int *mti,
               const uint32_t *mt);
 int gw_download(gw_ctx *ctx, double *frus, int *ltype, int *ryr, int *ito2, int *mti, uint32_t *mt);
+/* The same for FRUs first .. first+count-1 only (arrays indexed from 0):
+ * what write_fru_props (write_fru_props.c:28-128) reads at every output
+ * step, without the whole-cell gather of parallel_get_FRUs. */
+int gw_download_range(gw_ctx *ctx, int first, int count, double *frus, int *ltype, int *ryr, int *ito2);
 
 /* Seed every FRU's MT19937 on the device: scheme 0 = seed base+j,
  * scheme 1 = the formula of initialize_ran.c:30-34. */

@@ -87,6 +87,15 @@ int gw_download(gw_ctx *c, double *frus, int *ltype, int *ryr, int *ito2, int *m
     copy_set(&dst, &c->live, c->n);
     return GW_OK;
 }
+int gw_download_range(gw_ctx *c, int first, int count, double *frus, int *ltype, int *ryr, int *ito2)
+{
+    set_t src = {c->live.frus + 5 * first, c->live.ltype + 8 * first, c->live.ryr + 20 * first,
+                 c->live.ito2 + 4 * first, NULL, NULL};
+    set_t dst = {frus, ltype, ryr, ito2, NULL, NULL};
+    if (first < 0 || count <= 0 || first + count > c->n) return GW_EINVAL;
+    copy_set(&dst, &src, count);
+    return GW_OK;
+}
 int gw_seed(gw_ctx *c, int scheme, uint32_t base)
 {
     uint32_t *seeds = malloc(sizeof(uint32_t) * c->n);

@@ -105,3 +105,50 @@ def test_checkpoint_files(tmp_path, have_ref):
 def test_bad_settings_are_rejected(tmp_path):
     r = subprocess.run([cpu_driver(), "no_such_key=3"], cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode != 0 and "unknown setting" in r.stderr
+
+
+def _props_files(d):
+    return sorted(f for f in os.listdir(d) if f.startswith("fruprops"))
+
+
+def test_fru_props_files(tmp_path, have_ref):
+    """write_fru_props_flag = 1: fruprops_J / fruprops_avg_J / fruprops_avg_tot
+    files for FRUs fru_start..fru_end (write_fru_props.c:28-188).  With
+    fru_props_compat = 1 (the reference's swapped LType subscripts,
+    write_fru_props.c:90-91) every file equals the reference's byte for byte;
+    the default writes the cleft's own LCC flux, so there only the LCC flux
+    columns may differ, and each of its entries is 0 or the GHK flux of that
+    cleft at the step's V and CaSS."""
+    import numpy as np
+    m = build_ref.cfg_macros(250, 15.0)
+    m["write_fru_props_flag"] = 1
+    st = {"NFRU_sim": 250, "time_end": 15.0, "ic_file_flag": 0, "seed_scheme": 0, "seed_base": 5489,
+          "write_fru_props_flag": 1, "fru_start": 0, "fru_end": 9}
+    ref_dir, gw_dir = _run_both(tmp_path, m, dict(st, fru_props_compat=1), 5489)
+    files = _props_files(ref_dir)
+    assert len(files) == 21 and files == _props_files(gw_dir)
+    for f in files:
+        assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
+    fixed = tmp_path / "fixed"
+    fixed.mkdir()
+    subprocess.run([cpu_driver()] + ["%s=%s" % kv for kv in st.items()], cwd=fixed, check=True, capture_output=True)
+    V = np.loadtxt(fixed / "states.0.txt", skiprows=1)[:, 1]
+    RT_F, F, Vmyo, Cao = 8.314 * 310.0 / 96.5, 96.5, 25.84e-6, 2.0
+    PCa = 1.5 / 2.8 * 0.2 * 0.9 * 0.9468e-11
+    nonzero = 0
+    for f in files:
+        a = np.loadtxt(fixed / f, skiprows=1)
+        b = np.loadtxt(ref_dir / f, skiprows=1)
+        flux_col = 1
+        keep = [k for k in range(a.shape[1]) if k != flux_col]
+        assert np.array_equal(a[:, keep], b[:, keep]), f
+        if f.startswith("fruprops_") and not f.startswith("fruprops_avg"):
+            v = np.repeat(V, 4)
+            vf = v / RT_F
+            ghk = PCa * 4.0 * (1000.0 * F * vf) * (a[:, 5] * np.exp(2 * vf) - Cao * 0.341) / \
+                (np.exp(2 * vf) - 1.0) / (-2.0 * Vmyo * F * 1000.0)
+            j = a[:, flux_col]
+            on = j != 0.0
+            nonzero += int(on.sum())
+            assert np.allclose(j[on], ghk[on], rtol=2e-7, atol=0), f
+    assert nonzero > 0
