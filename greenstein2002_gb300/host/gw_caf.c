@@ -18,6 +18,18 @@
  * every Ndump output steps, and with write_fru_props_flag = 1 the per-FRU
  * property files fruprops_J.N.txt, fruprops_avg_J.N.txt and
  * fruprops_avg_tot.N.txt for FRUs fru_start..fru_end (write_fru_props.c).
+ *
+ * Exact checkpoints (exact_restart = 1): beside the reference's r_*.N.txt
+ * files, whose %g values cannot restart a run exactly, every checkpoint also
+ * writes r_exact.N.bin with the full-precision global and FRU state, every
+ * FRU's MT19937 words and position, the clock and the integrator's next step
+ * size.  restart_file = <path> resumes from one: the resumed run writes the
+ * same files, byte for byte, as the run that wrote the checkpoint went on to
+ * write.  The file is native-endian (both supported hosts are little-endian):
+ *   char magic[8] = "GWCKPT1"; int32 nfru, filenumber, iv_n, reserved;
+ *   double time, oldstep, iv_time, state[37];
+ *   double frus[n][5]; int32 ltype[n][4][2], ryr[n][4][5], ito2[n][4], mti[n];
+ *   uint32 mt[n][624].
  */
 #include <ctype.h>
 #include <math.h>
@@ -32,9 +44,9 @@
 typedef struct {
     gw_settings s;
     int nfru, ts_sec, ic_file_flag, Ndump, filenumber0, seed_scheme;
-    int write_fru_props_flag, fru_start, fru_end, fru_props_compat;
+    int write_fru_props_flag, fru_start, fru_end, fru_props_compat, exact_restart;
     unsigned long seed_base;
-    char ic_dir[512], output_dir[512];
+    char ic_dir[512], output_dir[512], restart_file[512];
     char ic_states[128], ic_FRU[128], ic_LCh[128], ic_RyR[128], ic_Ito2[128];
 } run_cfg;
 
@@ -98,9 +110,11 @@ static int set_key(run_cfg *c, const char *k, const char *v)
     if (!strcmp(k, "fru_start")) { c->fru_start = atoi(v); return 0; }
     if (!strcmp(k, "fru_end")) { c->fru_end = atoi(v); return 0; }
     if (!strcmp(k, "fru_props_compat")) { c->fru_props_compat = atoi(v); return 0; }
+    if (!strcmp(k, "exact_restart")) { c->exact_restart = atoi(v); return 0; }
 #define STR(field, name) if (!strcmp(k, name)) { snprintf(c->field, sizeof c->field, "%s", v); return 0; }
     STR(ic_dir, "ic_dir") STR(output_dir, "output_dir") STR(ic_states, "ic_states_file") STR(ic_FRU, "ic_FRU_file")
     STR(ic_LCh, "ic_LCh_file") STR(ic_RyR, "ic_RyR_file") STR(ic_Ito2, "ic_Ito2_file")
+    STR(restart_file, "restart_file")
 #undef STR
     return -1;
 }
@@ -295,6 +309,109 @@ static void restart_data(const run_cfg *c, int num, const double *state, gw_ctx 
     free(frus); free(ltype); free(ryr); free(ito2);
 }
 
+/* ---- exact checkpoints ------------------------------------------------------ */
+typedef struct {
+    char magic[8];
+    int32_t nfru, filenumber, iv_n, reserved;
+    double time, oldstep, iv_time, state[GW_NSTATE];
+} exact_header;
+
+static const char kExactMagic[8] = "GWCKPT1";
+
+static int write_all(FILE *f, const void *p, size_t size, size_t n) { return fwrite(p, size, n, f) == n ? 0 : -1; }
+static int read_all(FILE *f, void *p, size_t size, size_t n) { return fread(p, size, n, f) == n ? 0 : -1; }
+
+/* r_exact.<num>.bin: the state the run continues from, filenumber being the
+ * number its next output files take */
+static void write_exact(const run_cfg *c, int num, int filenumber, double time, double oldstep, double iv_time,
+                        const double *state, gw_ctx *ctx)
+{
+    const int n = c->nfru;
+    exact_header h;
+    char path[1200];
+    FILE *f;
+    double *frus = malloc(sizeof(double) * 5 * n);
+    int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n), *ito2 = malloc(sizeof(int) * 4 * n);
+    int *mti = malloc(sizeof(int) * n);
+    uint32_t *mt = malloc(sizeof(uint32_t) * 624 * (size_t)n);
+    int bad;
+    if (!frus || !ltype || !ryr || !ito2 || !mti || !mt || gw_download(ctx, frus, ltype, ryr, ito2, mti, mt)) {
+        fprintf(stderr, "exact checkpoint: download failed: %s\n", gw_last_error());
+        exit(4);
+    }
+    memset(&h, 0, sizeof h);
+    memcpy(h.magic, kExactMagic, 8);
+    h.nfru = n;
+    h.filenumber = filenumber;
+    h.iv_n = c->s.iv_n;
+    h.time = time;
+    h.oldstep = oldstep;
+    h.iv_time = iv_time;
+    memcpy(h.state, state, sizeof h.state);
+    snprintf(path, sizeof path, "%sr_exact.%d.bin", c->output_dir, num);
+    if (!(f = fopen(path, "wb"))) {
+        fprintf(stderr, "Cannot open file '%s'!\n", path);
+        exit(3);
+    }
+    bad = write_all(f, &h, sizeof h, 1) || write_all(f, frus, sizeof(double), 5 * (size_t)n) ||
+          write_all(f, ltype, sizeof(int), 8 * (size_t)n) || write_all(f, ryr, sizeof(int), 20 * (size_t)n) ||
+          write_all(f, ito2, sizeof(int), 4 * (size_t)n) || write_all(f, mti, sizeof(int), (size_t)n) ||
+          write_all(f, mt, sizeof(uint32_t), 624 * (size_t)n);
+    if (fclose(f) || bad) {
+        fprintf(stderr, "Cannot write file '%s'!\n", path);
+        exit(3);
+    }
+    free(frus); free(ltype); free(ryr); free(ito2); free(mti); free(mt);
+}
+
+/* Resume from an exact checkpoint: uploads the FRU and MT state and returns
+ * the clock, step size and file number the run continues with. */
+static void read_exact(run_cfg *c, gw_ctx *ctx, double *state, double *time, double *oldstep, double *iv_time,
+                       int *filenumber)
+{
+    const int n = c->nfru;
+    exact_header h;
+    FILE *f = fopen(c->restart_file, "rb");
+    double *frus = malloc(sizeof(double) * 5 * n);
+    int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n), *ito2 = malloc(sizeof(int) * 4 * n);
+    int *mti = malloc(sizeof(int) * n);
+    uint32_t *mt = malloc(sizeof(uint32_t) * 624 * (size_t)n);
+    if (!f) {
+        fprintf(stderr, "Cannot open file '%s'!\n", c->restart_file);
+        exit(2);
+    }
+    if (!frus || !ltype || !ryr || !ito2 || !mti || !mt) {
+        fprintf(stderr, "restart: out of host memory\n");
+        exit(4);
+    }
+    if (read_all(f, &h, sizeof h, 1) || memcmp(h.magic, kExactMagic, 8)) {
+        fprintf(stderr, "'%s' is not an exact checkpoint\n", c->restart_file);
+        exit(2);
+    }
+    if (h.nfru != n) {
+        fprintf(stderr, "'%s' holds %d FRUs, the run has %d\n", c->restart_file, (int)h.nfru, n);
+        exit(2);
+    }
+    if (read_all(f, frus, sizeof(double), 5 * (size_t)n) || read_all(f, ltype, sizeof(int), 8 * (size_t)n) ||
+        read_all(f, ryr, sizeof(int), 20 * (size_t)n) || read_all(f, ito2, sizeof(int), 4 * (size_t)n) ||
+        read_all(f, mti, sizeof(int), (size_t)n) || read_all(f, mt, sizeof(uint32_t), 624 * (size_t)n)) {
+        fprintf(stderr, "'%s' is truncated\n", c->restart_file);
+        exit(2);
+    }
+    fclose(f);
+    if (gw_upload(ctx, frus, ltype, ryr, ito2, mti, mt)) {
+        fprintf(stderr, "restart upload failed: %s\n", gw_last_error());
+        exit(5);
+    }
+    memcpy(state, h.state, sizeof h.state);
+    *time = h.time;
+    *oldstep = h.oldstep;
+    *iv_time = h.iv_time;
+    *filenumber = h.filenumber;
+    c->s.iv_n = h.iv_n;
+    free(frus); free(ltype); free(ryr); free(ito2); free(mti); free(mt);
+}
+
 /* ---- per-FRU property files (write_fru_props.c:28-188) ------------------- */
 typedef struct {
     FILE **fru, **avg, *tot;
@@ -481,7 +598,10 @@ int main(int argc, char **argv)
     gw_set_scale(ctx, 12500.0 / c.nfru);
     oldstep = c.s.step_max;
     filenumber = c.filenumber0;
-    init_cell(&c, ctx, state);
+    if (c.restart_file[0])
+        read_exact(&c, ctx, state, &c.s.time_start, &oldstep, &iv_time, &filenumber);
+    else
+        init_cell(&c, ctx, state);
     fst = open_states(&c, filenumber);
     fcu = open_currents(&c, filenumber);
     fot = open_otherstates(&c, filenumber);
@@ -534,6 +654,7 @@ int main(int argc, char **argv)
         if (n_restart >= c.Ndump) {
             n_restart = 0;
             restart_data(&c, filenumber, state, ctx);
+            if (c.exact_restart) write_exact(&c, filenumber, filenumber + 1, tstep, oldstep, iv_time, state, ctx);
             filenumber = filenumber + 1;
             fclose(fot);
             fclose(fst);

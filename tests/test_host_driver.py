@@ -152,3 +152,38 @@ def test_fru_props_files(tmp_path, have_ref):
             nonzero += int(on.sum())
             assert np.allclose(j[on], ghk[on], rtol=2e-7, atol=0), f
     assert nonzero > 0
+
+
+def _run_driver(exe, d, settings):
+    d.mkdir()
+    subprocess.run([exe] + ["%s=%s" % kv for kv in settings.items()], cwd=d, check=True, capture_output=True)
+
+
+def exact_restart_case(exe, tmp_path):
+    """A paced 250-FRU cell over [0, 20) ms with checkpoints every 8 ms, run
+    straight through and resumed from its first exact checkpoint: every file
+    the resumed run writes equals the straight run's byte for byte."""
+    base = {"NFRU_sim": 250, "time_end": 20.0, "ic_file_flag": 0, "seed_scheme": 0, "seed_base": 5489,
+            "Ndump": 8, "exact_restart": 1, "write_fru_props_flag": 1, "fru_start": 3, "fru_end": 5}
+    full, resumed = tmp_path / "full", tmp_path / "resumed"
+    _run_driver(exe, full, base)
+    _run_driver(exe, resumed, dict(base, restart_file=str(full / "r_exact.0.bin")))
+    written = sorted(os.listdir(resumed))
+    assert "states.1.txt" in written and "r_exact.1.bin" in written and "states.0.txt" not in written
+    for f in written:
+        assert filecmp.cmp(full / f, resumed / f, shallow=False), f
+    return written
+
+
+def test_exact_restart_continues_bit_for_bit(tmp_path):
+    exact_restart_case(cpu_driver(), tmp_path)
+
+
+def test_exact_restart_rejects_wrong_size(tmp_path):
+    exe = cpu_driver()
+    base = {"NFRU_sim": 64, "time_end": 3.0, "ic_file_flag": 0, "seed_scheme": 0, "Ndump": 2, "exact_restart": 1}
+    _run_driver(exe, tmp_path / "a", base)
+    r = subprocess.run([exe, "NFRU_sim=128", "time_end=3", "ic_file_flag=0",
+                        "restart_file=%s" % (tmp_path / "a" / "r_exact.0.bin")], cwd=tmp_path, capture_output=True,
+                       text=True)
+    assert r.returncode != 0 and "holds 64 FRUs" in r.stderr
