@@ -1,0 +1,92 @@
+"""Ensemble parity over 64 seeds (the reference's serial program vs the GPU
+path, NFRU=250, first beat at 1 Hz) and the mixed-precision check against
+the FP64 GPU run with the same seeds.
+
+FP64 vs the reference (stated tolerances): per-ms ensemble means of V within
+0.01 mV, of Cai within 1e-5 of its range, of JSR Ca within 1e-5 relative, of
+the LCC and RyR open probabilities within 1e-6; per seed, APD90 within
+0.01 ms and peak Cai within 1e-9 relative for at least 62 of the 64 seeds.
+
+Mixed vs FP64 (same seeds): the mean peak Cai within 1%, and the mean APD90
+within 1% or, where a 250-FRU cell's beat-to-beat noise is larger than that
+(APD90 spreads over 300-900 ms across seeds at this size), within three
+standard errors of the paired per-seed differences.
+(Seed k: FRU j seeded 5489 + 100000 k + j, as tests/golden/make_ensemble.py.)"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden
+
+sys.path.insert(0, GOLDEN)
+pytestmark = pytest.mark.gpu
+
+
+def run_ensemble(gw, prec, nseed, nfru, t_end, lockstep=True):
+    cells, sets, states = [], [], []
+    for k in range(nseed):
+        c = gw.Cell(nfru, precision=prec)
+        st = gw.settings()
+        states.append(c.init_rest(st, scheme=gw.SEED_BASE, base=5489 + 100000 * k))
+        cells.append(c)
+        sets.append(st)
+    states = np.ascontiguousarray(np.array(states))
+    b = gw.Batch(prec)
+    tr, ot = b.run(cells, sets, np.zeros(nseed), states, np.full(nseed, 0.1), int(t_end), traces=True,
+                    lockstep=lockstep)
+    for c in cells:
+        c.close()
+    b.close()
+    return tr, ot
+
+
+def summary(tr, ot):
+    import make_ensemble as me
+    n, m, _ = tr.shape
+    t = np.arange(1, m + 1, dtype=float)
+    st = np.concatenate([np.broadcast_to(t / 1000.0, (n, m))[:, :, None], tr], axis=2)
+    oth = np.concatenate([np.broadcast_to(t / 1000.0, (n, m))[:, :, None], ot], axis=2)
+    return me.summarise(st, oth)
+
+
+@pytest.fixture(scope="module")
+def fp64_run(gw):
+    g = golden("ensemble250.npz")
+    tr, ot = run_ensemble(gw, "fp64", int(g["nseed"][0]), int(g["nfru"][0]), 1000)
+    return g, summary(tr, ot)
+
+
+def test_ensemble_matches_reference(fp64_run):
+    g, s = fp64_run
+    dv = np.max(np.abs(s["V_mean"] - g["V_mean"]))
+    rng = g["Cai_mean"].max() - g["Cai_mean"].min()
+    dc = np.max(np.abs(s["Cai_mean"] - g["Cai_mean"])) / rng
+    djsr = np.max(np.abs(s["CaJSR_mean"] - g["CaJSR_mean"]) / g["CaJSR_mean"])
+    dplo = np.max(np.abs(s["PLType_open_mean"] - g["PLType_open_mean"]))
+    dpro = np.max(np.abs(s["PRyR_open_mean"] - g["PRyR_open_mean"]))
+    apd_same = int(np.sum(np.abs(s["apd90"] - g["apd90"]) < 0.01))
+    pk_same = int(np.sum(np.abs(s["peak_Cai"] - g["peak_Cai"]) <= 1e-9 * g["peak_Cai"]))
+    print("ensemble vs reference: |dV|max %.3g mV, dCai %.3g of range, dCaJSR %.3g, dPLCC %.3g, dPRyR %.3g, "
+          "APD90 equal in %d/64 seeds, peak Cai in %d/64" % (dv, dc, djsr, dplo, dpro, apd_same, pk_same))
+    assert dv < 0.01 and dc < 1e-5 and djsr < 1e-5 and dplo < 1e-6 and dpro < 1e-6
+    assert apd_same >= 62 and pk_same >= 62
+
+
+def test_mixed_precision_ensemble_vs_fp64(gw, fp64_run):
+    g, s = fp64_run
+    tr, ot = run_ensemble(gw, "mixed", int(g["nseed"][0]), int(g["nfru"][0]), 1000)
+    m = summary(tr, ot)
+    d_apd = m["apd90"] - s["apd90"]
+    d_pk = m["peak_Cai"] - s["peak_Cai"]
+    n = len(d_apd)
+    apd_rel = abs(d_apd.mean()) / s["apd90"].mean()
+    apd_tol = max(0.01, 3.0 * d_apd.std(ddof=1) / np.sqrt(n) / s["apd90"].mean())
+    pk_rel = abs(d_pk.mean()) / s["peak_Cai"].mean()
+    print("mixed vs fp64 over %d seeds: APD90 %+.3f%% (tolerance %.2f%%), peak Cai %+.3f%%, "
+          "seeds on the FP64 trajectory %d" % (n, 100 * d_apd.mean() / s["apd90"].mean(), 100 * apd_tol,
+                                               100 * d_pk.mean() / s["peak_Cai"].mean(),
+                                               int(np.sum(np.abs(d_apd) < 0.01))))
+    assert pk_rel < 0.01
+    assert apd_rel < apd_tol
