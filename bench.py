@@ -12,9 +12,12 @@ ms than the beat average, so the rate is a conservative one.  L2 (129 MB) is
 flushed by a 512 MB write between timed steps.
 
 Beside the FP64 value the line carries the same window in mixed precision
-("mixed", with its error against the FP64 run) and a batched run ("batched":
-many cells of NFRU 1250-12,500 with varied pacing and conductances sharing
-each stage launch, mixed precision).
+("mixed", with its error against the FP64 run), a batched run ("batched":
+64 cells of NFRU 1250-12,500 with varied pacing and conductances running
+concurrently, mixed precision) and a serving sweep ("serving": Poisson
+arrivals of cell requests, p50/p99 latency).  Before each timed section the
+launch-shape autotuner picks lanes per FRU and warps per block on the
+section's own workload ("tuning"; results do not depend on the choice).
 
 value: inputs resident in HBM, device-timed with CUDA events on the library's
 stream.  e2e: the same window through the C-ABI with host buffers: every
@@ -23,11 +26,15 @@ and downloads it and the step's traces (gw_download) inside the timed region.
 
 --impl reference: the reference's own serial program (oracle/_ref, built
 from its sources) on the host cores, one independent 12,500-FRU cell per
-core, each step a bounded 1-ms sample from rest.
+core, each step a bounded 1-ms sample per cell starting from the bench
+cell's state at 30, 80, 130 or 180 ms (tests/golden/ic_window), i.e. the
+phases of the timed window.  cpu_baseline: the same program on one core,
+1 ms from each of those four states.
 """
 import argparse
 import json
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -66,8 +73,11 @@ def parse():
     ap.add_argument("--batch-mode", default="streams", choices=["streams", "lockstep"],
                     help="streams: each cell on its own stream; lockstep: shared batched launches")
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[10.0, 50.0, 200.0])
-    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--tune-ms", type=float, default=2.0, help="simulated window per autotuner candidate")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[1.0, 10.0, 50.0, 200.0])
+    ap.add_argument("--serve-requests", type=int, default=48,
+                    help="requests per rate (at most rate x 24 s of arrivals, at least 16)")
     ap.add_argument("--serve-ms", type=float, default=20.0)
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
@@ -156,21 +166,39 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # reference (CPU) side
 # ---------------------------------------------------------------------------
-def reference_build(ms):
+WINDOW_IC = os.path.join(ROOT, "tests", "golden", "ic_window")
+
+
+def reference_build(ms, window_ic=False):
+    """The reference program built from its own sources for a 12,500-FRU cell
+    running `ms` simulated ms; window_ic = True starts it from the IC files in
+    ./ic (a phase of the GPU arm's timed window) instead of the rest state."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import build_ref
     if not build_ref.have_sources():
         return None, "reference sources not present (oracle/_ref/src missing)"
     try:
-        return build_ref.build_config("bench12500_%gms" % ms, build_ref.cfg_macros(NFRU, ms), lib=False,
-                                      exe=True), None
+        m = build_ref.cfg_macros(NFRU, ms)
+        name = "bench12500_%gms" % ms
+        if window_ic:
+            m.update({"ic_file_flag": 1, "ic_dir": '"ic"'})
+            name += "_ic"
+        return build_ref.build_config(name, m, lib=False, exe=True), None
     except Exception as e:  # noqa: BLE001
         return None, "reference build failed: %s" % str(e).splitlines()[0]
 
 
-def reference_sample(d, procs, ms, seed0):
+def window_phases():
+    if not os.path.isdir(WINDOW_IC):
+        return []
+    return [os.path.join(WINDOW_IC, d) for d in sorted(os.listdir(WINDOW_IC), key=lambda d: float(d[1:]))]
+
+
+def reference_sample(d, procs, ms, seed0, phases=None):
     """Run `procs` independent reference cells concurrently for `ms` simulated
-    ms each; returns (cell-ms/s, wall s)."""
+    ms each, cell p starting from IC phase p mod len(phases) when given;
+    returns (cell-ms/s, wall s)."""
+    phases = [p for p in (phases or []) if p]
     import resource
     import tempfile
 
@@ -179,10 +207,14 @@ def reference_sample(d, procs, ms, seed0):
 
     with tempfile.TemporaryDirectory() as tmp:
         ps = []
-        t0 = time.perf_counter()
         for p in range(procs):
             wd = os.path.join(tmp, str(p))
             os.makedirs(wd)
+            if phases:
+                shutil.copytree(phases[p % len(phases)], os.path.join(wd, "ic"))
+        t0 = time.perf_counter()
+        for p in range(procs):
+            wd = os.path.join(tmp, str(p))
             env = dict(os.environ, GW_SEED_BASE=str(seed0 + p * NFRU))
             ps.append(subprocess.Popen([os.path.join(d, "stoch")], cwd=wd, env=env, stdout=subprocess.DEVNULL,
                                        stderr=subprocess.PIPE, preexec_fn=_stack))
@@ -195,29 +227,38 @@ def reference_sample(d, procs, ms, seed0):
 
 
 def run_reference(args, dist):
+    """The reference program on all host cores, one independent 12,500-FRU cell
+    per core, each step 1 simulated ms per cell.  The cells start from the
+    bench cell's state at 30, 80, 130 and 180 ms (tests/golden/ic_window, in
+    turn), so the sample covers the phases of the GPU arm's timed window
+    rather than the cheaper rest state."""
     if dist.rank != 0:
         return
     ms = 1.0
-    d, why = reference_build(ms)
+    phases = window_phases()
+    d, why = reference_build(ms, window_ic=bool(phases))
     if d is None:
         print(json.dumps({"impl": "reference", "unavailable": why}))
         return
     procs = os.cpu_count() or 1
     for _ in range(args.warmup):
-        reference_sample(d, procs, ms, SEED)
+        reference_sample(d, procs, ms, SEED, phases)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        reference_sample(d, procs, ms, SEED)
+        reference_sample(d, procs, ms, SEED, phases)
     wall = time.perf_counter() - t0
     value = args.steps * procs * ms / wall
+    start = ("from the bench cell's state at %s ms (IC files, first 1250 FRUs replicated as the reference "
+             "reads them)" % "/".join(os.path.basename(p)[1:] for p in phases)) if phases else "from rest"
     sample = ("reference program (caf.c, serial build of its own sources, gcc -O3) x%d concurrent cells, "
-              "NFRU=12,500 each, 1 ms from rest per cell per step" % procs)
+              "NFRU=12,500 each, 1 ms per cell per step, %s" % (procs, start))
     print(json.dumps({
         "impl": "reference", "metric": "cell-ms simulated/s at 12,500 FRUs", "value": value,
         "unit": "cell-ms/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "one 12,500-FRU cell per host core, rest state, 1 Hz pacing, seeds 5489+j",
+        "config": {"workload": "one 12,500-FRU cell per host core, 1 Hz pacing, seeds 5489+j, 1-ms samples of "
+                               "the phases of the window [30, 230) ms",
                    "nfru": NFRU, "cells": procs, "ms_per_cell_per_step": ms},
         "cpu_baseline": {"value": value, "unit": "cell-ms/s", "cores": procs, "kind": "reference",
                          "sample": sample},
@@ -242,6 +283,13 @@ def load_peaks():
         return {}
 
 
+def tune_summary(res, args):
+    lanes, warps, ms = res
+    return {"lanes_per_fru": lanes, "fru_per_warp": 32 // lanes, "warps_per_block": warps,
+            "window_ms": args.tune_ms,
+            "candidates_ms": {"%d_lanes_%d_warps" % k: round(v, 2) for k, v in sorted(ms.items())}}
+
+
 def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
     """Device-resident run of one cell: warm-up, then K timed steps with CUDA
     events on the library's stream.  Returns the measurements."""
@@ -253,6 +301,10 @@ def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
     for _ in range(args.warmup):
         t, _, _, _ = cell.run(state, t, n, oldstep, st, want=())
         oldstep = cell.oldstep
+    tuning = None
+    if not args.no_autotune and args.fru_lanes == 4:
+        # launch shape picked on this cell's own workload (same results either way)
+        tuning = tune_summary(G.autotune([cell], [st], [t], state[None, :], [oldstep], args.tune_ms), args)
     sub0, launch0 = cell.substeps(), cell.launches()
     cell.profile(True)
     total_ms = 0.0
@@ -275,17 +327,20 @@ def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
     dist.barrier()
     kern_ms, kern_launches = cell.profile_read()
     out = {"wall_ms": dist.max(total_ms), "substeps": cell.substeps() - sub0, "launches": cell.launches() - launch0,
-           "kern_ms": kern_ms, "kern_launches": kern_launches, "clocks": clk,
+           "kern_ms": kern_ms, "kern_launches": kern_launches, "clocks": clk, "tuning": tuning,
            "trace": np.concatenate(trace) if keep_trace else None}
     out["value"] = dist.sum(args.steps * args.step_ms) / (out["wall_ms"] / 1000.0)
     cell.close()
     return out
 
 
-def time_e2e(G, args, dist, seed):
+def time_e2e(G, args, dist, seed, tuning=None):
     """The same window through the C-ABI with host buffers: the cell's full FRU +
     RNG state is uploaded and downloaded, and its traces read back, every step."""
     cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, args.precision)
+    if tuning:
+        cell.set_fru_lanes(tuning["lanes_per_fru"])
+        cell.set_stage_warps(tuning["warps_per_block"])
     t = 0.0
     oldstep = st.step_max
     n = int(args.step_ms)
@@ -335,6 +390,9 @@ def time_batched(G, args, dist):
     b = G.Batch("mixed")
     lock = args.batch_mode == "lockstep"
     b.run(cells, sets, t, states, old, args.batch_warmup_ms, lockstep=lock)
+    tuning = None
+    if not args.no_autotune:
+        tuning = tune_summary(G.autotune(cells, sets, t, states, old, args.tune_ms, batch=b if lock else None), args)
     sub0 = sum(c.substeps() for c in cells)
     b.profile(True)
     launch0 = sum(c.launches() for c in cells)
@@ -356,7 +414,7 @@ def time_batched(G, args, dist):
             "nfru_mix": {str(k): int(np.sum(sizes == k)) for k in (1250, 2500, 5000, 12500)},
             "window_ms": [args.batch_warmup_ms, args.batch_warmup_ms + args.batch_ms],
             "fru_substeps_per_s": substeps / wall, "batched_launches": int(launches),
-            "kernel_ms": kern_ms, "precision": "mixed", "mode": args.batch_mode,
+            "kernel_ms": kern_ms, "precision": "mixed", "mode": args.batch_mode, "tuning": tuning,
             "timing": "host wall clock around the batched run (one host thread per cell)"}
 
 
@@ -368,7 +426,7 @@ def time_serving(G, args, rate):
     mixed precision, admitted by device bytes."""
     import numpy as np
     rng = np.random.default_rng(int(rate * 1000) + 7)
-    n = args.serve_requests
+    n = max(16, min(args.serve_requests, int(rate * 24)))
     srv = G.Server("mixed", slots=args.serve_slots, mem_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
                    lockstep=args.batch_mode == "lockstep")
     reqs = []
@@ -432,7 +490,7 @@ def run_gpu(args, dist):
         a, b = main["trace"], m["trace"]
         cai_range = float(np.max(a[:, 6]) - np.min(a[:, 6])) or 1.0
         mixed = {"value": m["value"], "unit": "cell-ms/s", "speedup_vs_fp64": m["value"] / main["value"],
-                 "fru_substeps_per_s": m["substeps"] / (m["wall_ms"] / 1000.0),
+                 "fru_substeps_per_s": m["substeps"] / (m["wall_ms"] / 1000.0), "tuning": m["tuning"],
                  "error_vs_fp64_same_seeds": {
                      "max_abs_dV_mV": float(np.max(np.abs(a[:, 0] - b[:, 0]))),
                      "max_abs_dCai_rel_to_range": float(np.max(np.abs(a[:, 6] - b[:, 6]))) / cai_range,
@@ -446,18 +504,20 @@ def run_gpu(args, dist):
                                "%d worker slots, %g GB admission budget" % (args.serve_ms, args.serve_slots,
                                                                             args.serve_budget_gb),
                    "sweep": [time_serving(G, args, r) for r in args.serve_rates]}
-    e2e = None if args.no_e2e else time_e2e(G, args, dist, seed)
+    e2e = None if args.no_e2e else time_e2e(G, args, dist, seed, main["tuning"])
 
     # ---- CPU baseline: the reference program on one host core ----
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        d, why = reference_build(3.0)
+        phases = window_phases()
+        d, why = reference_build(1.0, window_ic=bool(phases))
         if d is not None:
-            v, wall = reference_sample(d, 1, 3.0, SEED)
+            walls = [reference_sample(d, 1, 1.0, SEED, [ph])[1] for ph in (phases or [None])]
+            v = len(walls) / sum(walls)
             cpu = {"value": v, "unit": "cell-ms/s", "cores": 1, "kind": "reference",
-                   "sample": "reference program (serial build of its own sources), NFRU=12,500, rest state, "
-                             "first 3 ms (%.1f s wall); rest costs fewer substeps per ms than the plateau "
-                             "window timed on the GPU" % wall}
+                   "sample": "reference program (serial build of its own sources), NFRU=12,500, 1 ms from the "
+                             "bench cell's state at each of %s ms of the timed window (%.1f s wall in all)"
+                             % ("/".join(os.path.basename(p)[1:] for p in phases) or "0", sum(walls))}
         else:
             cpu = {"value": None, "unit": "cell-ms/s", "cores": 0, "kind": "reference", "sample": why}
 
@@ -492,6 +552,7 @@ def run_gpu(args, dist):
                                       "frac": achieved_gbs / hbm_peak,
                                       "algorithmic": "%g B x FRU-substeps" % BYTES_PER_SUBSTEP}},
             "clocks": main["clocks"],
+            "tuning": main["tuning"],
             "mixed": mixed,
             "batched": batched,
             "serving": serving,
