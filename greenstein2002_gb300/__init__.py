@@ -99,6 +99,12 @@ def bind(path):
         "gw_substeps": ([vp, P(C.c_ulonglong)], C.c_int),
         "gw_sync": ([vp], C.c_int),
         "gw_set_fru_lanes": ([vp, C.c_int], C.c_int),
+        "gw_set_stage_warps": ([vp, C.c_int], C.c_int),
+        "gw_stage_trace": ([vp, C.c_int], C.c_int),
+        "gw_stage_trace_read": ([vp, vp, vp], C.c_int),
+        "gw_batch_set_warps": ([vp, C.c_int], C.c_int),
+        "gw_autotune": ([C.c_int, vp, vp, _dp, _dp, _dp, C.c_double, vp, P(C.c_int), P(C.c_int), _dp], C.c_int),
+        "gw_download_range": ([vp, C.c_int, C.c_int, _dp, _ip, _ip, _ip], C.c_int),
         "gw_set_precision": ([vp, C.c_int], C.c_int),
         "gw_set_pca_scale": ([vp, C.c_double], C.c_int),
         "gw_settings_init": ([P(Settings)], None),
@@ -160,7 +166,8 @@ def _ptr(a):
 class Cell:
     """Device-resident FRU state of one cell (a gw_ctx)."""
 
-    def __init__(self, nfru, nfru_scale=None, lib=None, fru_lanes=None, precision=None, pca_scale=None):
+    def __init__(self, nfru, nfru_scale=None, lib=None, fru_lanes=None, precision=None, pca_scale=None,
+                 stage_warps=None):
         self._L = L = lib if lib is not None else load()
         self._h = C.c_void_p()
         _check(L.gw_create(C.byref(self._h), int(nfru)), "gw_create", self._L)
@@ -173,6 +180,25 @@ class Cell:
             _check(L.gw_set_pca_scale(self._h, float(pca_scale)), "gw_set_pca_scale", self._L)
         if fru_lanes is not None and hasattr(L, "gw_set_fru_lanes"):
             _check(L.gw_set_fru_lanes(self._h, int(fru_lanes)), "gw_set_fru_lanes", self._L)
+        if stage_warps is not None:
+            self.set_stage_warps(stage_warps)
+
+    def set_stage_warps(self, warps):
+        _check(self._L.gw_set_stage_warps(self._h, int(warps)), "gw_set_stage_warps", self._L)
+
+    def stage_trace(self, enable=True):
+        _check(self._L.gw_stage_trace(self._h, 1 if enable else 0), "gw_stage_trace", self._L)
+
+    def stage_trace_read(self):
+        """(substeps per FRU, per-warp [begin, end] ns) of the last stage launch."""
+        sub = np.zeros(self.nfru, np.uint32)
+        ns = np.zeros(((self.nfru + 7) // 8, 2), np.uint64)
+        _check(self._L.gw_stage_trace_read(self._h, sub.ctypes.data_as(C.c_void_p), ns.ctypes.data_as(C.c_void_p)),
+               "gw_stage_trace_read", self._L)
+        return sub, ns
+
+    def set_fru_lanes(self, lanes):
+        _check(self._L.gw_set_fru_lanes(self._h, int(lanes)), "gw_set_fru_lanes", self._L)
 
     def close(self):
         if self._h:
@@ -317,6 +343,9 @@ class Batch:
         except Exception:
             pass
 
+    def set_warps(self, warps):
+        _check(self._L.gw_batch_set_warps(self._h, int(warps)), "gw_batch_set_warps", self._L)
+
     def profile(self, enable=True):
         ms, n = C.c_double(0.0), C.c_ulonglong(0)
         _check(self._L.gw_batch_profile(self._h, 1 if enable else 0, C.byref(ms), C.byref(n)), "gw_batch_profile",
@@ -380,3 +409,25 @@ class Server:
 
 def cell_bytes(nfru):
     return int(load().gw_cell_bytes(int(nfru)))
+
+
+TUNE_CANDIDATES = ((4, 1), (4, 2), (4, 4), (4, 8), (1, 1))
+
+
+def autotune(cells, sets, t, states, oldsteps, window_ms, batch=None, lib=None):
+    """Launch-shape autotuner (gw_autotune): times window_ms of the cells' own
+    workload per (lanes per FRU, warps per block) candidate, restores their
+    state and sets the fastest.  Returns (lanes, warps, {candidate: ms})."""
+    L = lib if lib is not None else cells[0]._L
+    n = len(cells)
+    handles = (C.c_void_p * n)(*[c._h.value for c in cells])
+    setarr = (Settings * n)(*sets)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    states = np.ascontiguousarray(states, dtype=np.float64).reshape(n, NSTATE)
+    oldsteps = np.ascontiguousarray(oldsteps, dtype=np.float64)
+    ms = np.zeros(len(TUNE_CANDIDATES))
+    lanes, warps = C.c_int(0), C.c_int(0)
+    _check(L.gw_autotune(n, C.cast(handles, C.c_void_p), C.cast(setarr, C.c_void_p), t, states, oldsteps,
+                         float(window_ms), batch._h if batch is not None else None, C.byref(lanes), C.byref(warps),
+                         ms), "gw_autotune", L)
+    return lanes.value, warps.value, {c: float(m) for c, m in zip(TUNE_CANDIDATES, ms) if m >= 0.0}

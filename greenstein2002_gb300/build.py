@@ -30,6 +30,7 @@ CUDA_UNITS = {
     "gw_abi.cu": [],
     "gw_probe.cu": [],
     "gw_noalloc.cu": ["-fmad=false"],
+    "gw_tune.cu": [],
 }
 C_UNITS = ["gw_dp.c", "gw_dropin.c"]
 

@@ -37,8 +37,9 @@ static int set_err(int code, const char* fmt, ...) {
   } while (0)
 
 static cudaError_t launch_stage_variant(gw_ctx* c, const StageParams& p) {
-  if (c->precision == 1) return gw::launch_stage_mixed(c->d, p, c->stream);
-  return c->fru_lanes == 4 ? gw::launch_stage4(c->d, p, c->stream) : gw::launch_stage(c->d, p, c->stream);
+  if (c->precision == 1) return gw::launch_stage_mixed(c->d, p, c->stage_warps, c->stream);
+  return c->fru_lanes == 4 ? gw::launch_stage4(c->d, p, c->stage_warps, c->stream)
+                           : gw::launch_stage(c->d, p, c->stream);
 }
 
 extern "C" const char* gw_last_error(void) { return g_err; }
@@ -50,7 +51,8 @@ extern "C" int gw_nfru(const gw_ctx* c) { return c ? c->d.nfru : 0; }
 
 static void free_dev(gw_ctx* c) {
   void* ptrs[] = {c->d.frus, c->d.chan, c->d.mti, c->d.mt, c->d.frus_s, c->d.chan_s, c->d.mti_s,
-                  c->d.mt_hold, c->d.hold_epoch, c->d.partials, c->d.ticket, c->d.out, c->d.substeps};
+                  c->d.mt_hold, c->d.hold_epoch, c->d.partials, c->d.ticket, c->d.out, c->d.substeps,
+                  c->d.trace_sub, c->d.trace_ns};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -135,6 +137,13 @@ extern "C" int gw_set_fru_lanes(gw_ctx* c, int lanes) {
   if (lanes == 1 && (c->precision != 0 || c->pca_scale != 1.0))
     return set_err(GW_EINVAL, "gw_set_fru_lanes: the one-thread-per-FRU kernel is FP64 with the reference PCa only");
   c->fru_lanes = lanes;
+  return GW_OK;
+}
+
+extern "C" int gw_set_stage_warps(gw_ctx* c, int warps) {
+  if (!c || warps < 1 || warps > gw::kMaxStageWarps || (warps & (warps - 1)))
+    return set_err(GW_EINVAL, "gw_set_stage_warps: warps per block must be 1, 2, 4 or 8");
+  c->stage_warps = warps;
   return GW_OK;
 }
 
@@ -396,6 +405,43 @@ extern "C" int gw_resume(gw_ctx* c) {
 extern "C" int gw_substeps(gw_ctx* c, unsigned long long* count) {
   if (!c || !count) return set_err(GW_EINVAL, "gw_substeps: null argument");
   CK(cudaMemcpyAsync(count, c->d.substeps, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return GW_OK;
+}
+
+extern "C" int gw_stage_trace(gw_ctx* c, int enable) {
+  if (!c) return set_err(GW_EINVAL, "gw_stage_trace: null context");
+  if (c->batch) return set_err(GW_EINVAL, "gw_stage_trace: change it before the cell joins a batch");
+  CK(cudaStreamSynchronize(c->stream));
+  if (enable && !c->d.trace_sub) {
+    const size_t ng = (size_t)(c->d.nfru + 7) / 8;
+    CK(cudaMalloc((void**)&c->d.trace_sub, sizeof(uint32_t) * c->d.nfru));
+    cudaError_t e = cudaMalloc((void**)&c->d.trace_ns, sizeof(unsigned long long) * 2 * ng);
+    if (e != cudaSuccess) {
+      cudaFree(c->d.trace_sub);
+      c->d.trace_sub = nullptr;
+      CK(e);
+    }
+    CK(cudaMemsetAsync(c->d.trace_sub, 0, sizeof(uint32_t) * c->d.nfru, c->stream));
+    CK(cudaMemsetAsync(c->d.trace_ns, 0, sizeof(unsigned long long) * 2 * ng, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  } else if (!enable && c->d.trace_sub) {
+    cudaFree(c->d.trace_sub);
+    cudaFree(c->d.trace_ns);
+    c->d.trace_sub = nullptr;
+    c->d.trace_ns = nullptr;
+  }
+  return GW_OK;
+}
+
+extern "C" int gw_stage_trace_read(gw_ctx* c, uint32_t* substeps, unsigned long long* warp_ns) {
+  if (!c || !c->d.trace_sub) return set_err(GW_EINVAL, "gw_stage_trace_read: tracing is not enabled");
+  const size_t ng = (size_t)(c->d.nfru + 7) / 8;
+  if (substeps)
+    CK(cudaMemcpyAsync(substeps, c->d.trace_sub, sizeof(uint32_t) * c->d.nfru, cudaMemcpyDeviceToHost, c->stream));
+  if (warp_ns)
+    CK(cudaMemcpyAsync(warp_ns, c->d.trace_ns, sizeof(unsigned long long) * 2 * ng, cudaMemcpyDeviceToHost,
+                       c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return GW_OK;
 }

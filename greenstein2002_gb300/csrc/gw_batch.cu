@@ -39,6 +39,7 @@ struct gw_batch {
   unsigned long long round = 0;
   bool dirty = true;
   int nblocks = 0;
+  int warps = 1;  // warps per block of the batched launches
   int cap = 0;  // capacity of the device/pinned arrays (cells)
   gw::DevState* d_cells = nullptr;
   gw::StageParams* d_params = nullptr;
@@ -108,7 +109,7 @@ static cudaError_t launch_round(gw_batch* b) {
     for (int i = 0; i < n; i++) {
       b->h_cells[i] = b->members[i]->d;
       b->h_block0[i] = acc;
-      acc += (b->members[i]->d.nfru + 7) / 8;
+      acc += gw::stage_blocks(b->members[i]->d.nfru, b->warps);
     }
     b->h_block0[n] = acc;
     b->nblocks = acc;
@@ -128,8 +129,8 @@ static cudaError_t launch_round(gw_batch* b) {
   a.outs = b->d_outs;
   a.ncells = n;
   if (b->profiling) cudaEventRecord(b->ev[0], b->stream);
-  e = (b->precision == 1) ? gw::launch_stage_mixed_batch(a, b->nblocks, b->stream)
-                          : gw::launch_stage4_batch(a, b->nblocks, b->stream);
+  e = (b->precision == 1) ? gw::launch_stage_mixed_batch(a, b->nblocks, b->warps, b->stream)
+                          : gw::launch_stage4_batch(a, b->nblocks, b->warps, b->stream);
   if (e != cudaSuccess) return e;
   b->launches++;
   if (b->profiling) cudaEventRecord(b->ev[1], b->stream);
@@ -206,6 +207,17 @@ extern "C" int gw_batch_destroy(gw_batch* b) {
   cudaEventDestroy(b->ev[1]);
   cudaStreamDestroy(b->stream);
   delete b;
+  return GW_OK;
+}
+
+extern "C" int gw_batch_set_warps(gw_batch* b, int warps) {
+  if (!b || warps < 1 || warps > gw::kMaxStageWarps || (warps & (warps - 1)))
+    return gw_internal_error(GW_EINVAL, "gw_batch_set_warps: warps per block must be 1, 2, 4 or 8");
+  std::lock_guard<std::mutex> lk(b->mu);
+  if (b->warps != warps) {
+    b->warps = warps;
+    b->dirty = true;  // block prefix sums change
+  }
   return GW_OK;
 }
 

@@ -483,49 +483,71 @@ __device__ __forceinline__ void advance4(const StageCtx& sc, const Group& g, dou
   }
 }
 
-// Last-block pass of one cell whose blocks are bidx = 0..nblocks-1 of a
-// (possibly multi-cell) grid: partial sums in fixed block order.
+// Sum over the 32 lanes of a warp: one fixed shuffle tree.
 template <int NV>
-__device__ __forceinline__ bool cell_finish(const double v[NV], double* partials, unsigned* ticket, double* smem,
-                                            double tot[NV], int bidx, int nblocks) {
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
+__device__ __forceinline__ void warp_sum(double v[NV]) {
 #pragma unroll
-    for (int k = 0; k < NV; k++) partials[bidx * NV + k] = v[k];
+  for (int k = 0; k < NV; k++)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+}
+
+// Cross-FRU sums of one cell, independent of the launch shape: every warp
+// (8 FRUs, group grp of the cell's ngroups) stores its warp total, and the
+// last warp to arrive adds the group totals in a fixed lane-strided order
+// and one warp tree.  Whatever the warps per block, the sums are the same
+// bits.  Returns true in lane 0 of that last warp, with the totals in tot[].
+template <int NV>
+__device__ __forceinline__ bool cell_finish(const double v[NV], double* partials, unsigned* ticket, double tot[NV],
+                                            int grp, int ngroups) {
+  const int lane = threadIdx.x & 31;
+  unsigned last = 0u;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) partials[grp * NV + k] = v[k];
     __threadfence();
-    last = (atomicAdd(ticket, 1u) == (unsigned)nblocks - 1u);
+    last = (atomicAdd(ticket, 1u) == (unsigned)ngroups - 1u) ? 1u : 0u;
   }
-  __syncthreads();
+  last = __shfl_sync(0xffffffffu, last, 0);
   if (!last) return false;
   __threadfence();
   double s[NV];
 #pragma unroll
   for (int k = 0; k < NV; k++) s[k] = 0.0;
-  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+  for (int b = lane; b < ngroups; b += 32)
 #pragma unroll
     for (int k = 0; k < NV; k++) s[k] += __ldcg(&partials[b * NV + k]);
-  block_reduce<NV>(s, smem);
-  if (threadIdx.x == 0) {
+  warp_sum<NV>(s);
+  if (lane == 0) {
     *ticket = 0u;
 #pragma unroll
     for (int k = 0; k < NV; k++) tot[k] = s[k];
   }
-  return threadIdx.x == 0;
+  return lane == 0;
 }
 
-// The stage of one cell, block bidx of its nblocks: load, optional snapshot
-// save/restore, advance, store, and the fused deterministic flux reduction
+// The stage of one cell, block bidx of the cell's blocks (blockDim.x / 32
+// warps of 8 FRUs each): load, optional snapshot save/restore, advance,
+// store, and the fused deterministic flux reduction
 // (calc_fru_flux_local.c:28-77, mpi_master.c:447-468, mpi_slave.c:150-226);
 // the cell's totals go to out[0..8] and its error flag to out[kOutError].
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 template <typename R>
-__device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, int bidx, int nblocks, double* out) {
-  __shared__ double smem[32 * 5];
+__device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, int bidx, double* out) {
   const int lane = threadIdx.x & 31;
+  const int grp = bidx * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+  const int ngroups = (s.nfru + 7) >> 3;
+  if (grp >= ngroups) return;  // whole warps past the cell's last FRU
+  if (s.trace_ns && lane == 0) s.trace_ns[2 * grp] = global_ns();
   Group g;
   g.c = lane & 3;
   g.base = lane & ~3;
   g.mask = 0xfu << g.base;
-  const int f = bidx * 8 + (threadIdx.x >> 2);
+  const int f = grp * 8 + (lane >> 2);
   double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   uint32_t nsub = 0;
   bool overflow = false;
@@ -561,6 +583,7 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, in
       s.chan_s[g.c * nf + f] = w;
     }
     if (p.flags & kFlagAdvance) advance4<R>(sc, g, cajsr, cass, w, mti, nsub, overflow);
+    if (s.trace_sub && g.c == 0) s.trace_sub[f] = nsub;
     if (g.c == 0) {
       s.frus[f] = cajsr;
       s.mti[f] = mti;
@@ -576,15 +599,16 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, in
     if (cl_of(w) == 2) v[4] = 1.0;
   }
   __syncwarp();
+  if (s.trace_ns && lane == 0) s.trace_ns[2 * grp + 1] = global_ns();
   if (overflow) out[kOutError] = 1.0;
   if (s.substeps) {
     unsigned long long c = (g.c == 0) ? nsub : 0;
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
     if (lane == 0 && c) atomicAdd(s.substeps, c);
   }
-  block_reduce<5>(v, smem);
+  warp_sum<5>(v);
   double tot[5];
-  if (cell_finish<5>(v, s.partials, s.ticket, smem, tot, bidx, nblocks)) {
+  if (cell_finish<5>(v, s.partials, s.ticket, tot, grp, ngroups)) {
     double cur[4];
     currents_from_sums(s.nfru, p.nfru_scale, p.depf, tot, cur);
     cur[2] = cur[2] * p.pca_scale;  // ICa is proportional to the LCC permeability
@@ -596,8 +620,8 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, in
 }
 
 // ---- many cells in one launch ------------------------------------------------
-// Cell i owns blocks block0[i] .. block0[i+1]-1 of the grid (8 FRUs each);
-// its parameters are params[i] and its totals go to outs[i*32 ..].
+// Cell i owns blocks block0[i] .. block0[i+1]-1 of the grid (8 FRUs per
+// warp); its parameters are params[i] and its totals go to outs[i*32 ..].
 template <typename R>
 __device__ __forceinline__ void batch_body(const BatchArgs& a) {
   // the cell of this block: binary search of the block prefix sums
@@ -611,7 +635,7 @@ __device__ __forceinline__ void batch_body(const BatchArgs& a) {
   DevState s = a.cells[lo];
   const StageParams p = a.params[lo];
   if (p.flags < 0) return;  // the cell posted no operation this round
-  stage_body<R>(s, p, b - a.block0[lo], a.block0[lo + 1] - a.block0[lo], a.outs + kBatchOutStride * lo);
+  stage_body<R>(s, p, b - a.block0[lo], a.outs + kBatchOutStride * lo);
 }
 
 }  // namespace cleft

@@ -9,20 +9,20 @@
 
 namespace gw {
 
-__global__ void __launch_bounds__(32) fru_stage_mixed_kernel(DevState s, StageParams p) {
-  cleft::stage_body<float>(s, p, blockIdx.x, gridDim.x, s.out);
+__global__ void __launch_bounds__(kMaxStageWarps * 32) fru_stage_mixed_kernel(DevState s, StageParams p) {
+  cleft::stage_body<float>(s, p, blockIdx.x, s.out);
 }
 
-cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, cudaStream_t st) {
-  const int blocks = (s.nfru + 7) / 8;
-  fru_stage_mixed_kernel<<<blocks, 32, 0, st>>>(s, p);
+cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, int warps, cudaStream_t st) {
+  const int blocks = stage_blocks(s.nfru, warps);
+  fru_stage_mixed_kernel<<<blocks, 32 * warps, 0, st>>>(s, p);
   return cudaGetLastError();
 }
 
-__global__ void __launch_bounds__(32) fru_stage_mixed_batch_kernel(BatchArgs a) { cleft::batch_body<float>(a); }
+__global__ void __launch_bounds__(kMaxStageWarps * 32) fru_stage_mixed_batch_kernel(BatchArgs a) { cleft::batch_body<float>(a); }
 
-cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, cudaStream_t st) {
-  fru_stage_mixed_batch_kernel<<<nblocks, 32, 0, st>>>(a);
+cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, int warps, cudaStream_t st) {
+  fru_stage_mixed_batch_kernel<<<nblocks, 32 * warps, 0, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -22,10 +22,25 @@
 
 namespace gw {
 
+// Flux numerators of the cell, summed in exactly the order of the
+// cleft-parallel kernels (gw_fru_cleft.cuh), so every stage kernel gives the
+// same bits: per 8-FRU group and cleft a fixed tree over the FRUs
+// ((x0+x4)+(x2+x6))+((x1+x5)+(x3+x7)), then (S0+S2)+(S1+S3) over the clefts,
+// then the lane-strided last-warp pass over the groups.
+__device__ __forceinline__ double group8_sum(double x) {
+  x += __shfl_down_sync(0xffffffffu, x, 4);
+  x += __shfl_down_sync(0xffffffffu, x, 2);
+  x += __shfl_down_sync(0xffffffffu, x, 1);
+  return x;  // valid in lanes 0, 8, 16, 24
+}
+
 __global__ void __launch_bounds__(kStageThreads) fru_stage_kernel(DevState s, StageParams p) {
-  __shared__ double smem[32 * 5];
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  double x[kClefts][5];
+#pragma unroll
+  for (int c = 0; c < kClefts; c++)
+#pragma unroll
+    for (int k = 0; k < 5; k++) x[c][k] = 0.0;
   uint32_t nsub = 0;
   bool overflow = false;
   if (f < s.nfru) {
@@ -71,17 +86,17 @@ __global__ void __launch_bounds__(kStageThreads) fru_stage_kernel(DevState s, St
 #pragma unroll
     for (int c = 0; c < kClefts; c++) s.chan[c * nf + f] = w[c];
     s.mti[f] = rng.mti;
-    // flux numerators of this FRU (calc_fru_flux_local.c:45-70)
+    // flux numerators of this FRU's clefts (calc_fru_flux_local.c:45-70)
 #pragma unroll
     for (int c = 0; c < kClefts; c++) {
-      v[0] += y[c + 1];
+      x[c][0] = y[c + 1];
       if (lcc_open(w[c])) {
-        v[2] += y[c + 1];
-        v[3] += 1.0;
+        x[c][2] = y[c + 1];
+        x[c][3] = 1.0;
       }
-      if (cl_of(w[c]) == 2) v[4] += 1.0;
+      if (cl_of(w[c]) == 2) x[c][4] = 1.0;
     }
-    v[1] = y[0];
+    x[0][1] = y[0];
   }
   if (s.substeps) {
     // substep counter (workload accounting): warp-aggregated atomic
@@ -89,9 +104,39 @@ __global__ void __launch_bounds__(kStageThreads) fru_stage_kernel(DevState s, St
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(s.substeps, c);
   }
-  block_reduce<5>(v, smem);
-  double tot[5];
-  if (grid_finish<5>(v, s.partials, s.ticket, smem, tot)) {
+  double v[5];
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    const double s0 = group8_sum(x[0][k]), s1 = group8_sum(x[1][k]);
+    const double s2 = group8_sum(x[2][k]), s3 = group8_sum(x[3][k]);
+    v[k] = (s0 + s2) + (s1 + s3);
+  }
+  // lanes 0, 8, 16, 24 hold the totals of their 8-FRU groups
+  const int lane = threadIdx.x & 31;
+  const int ngroups = (s.nfru + 7) >> 3, grp0 = (blockIdx.x * blockDim.x) >> 3;
+  const int mine = min(4, ngroups - grp0);  // groups of this warp that hold FRUs
+  unsigned last = 0u;
+  if ((lane & 7) == 0 && (lane >> 3) < mine) {
+#pragma unroll
+    for (int k = 0; k < 5; k++) s.partials[(grp0 + (lane >> 3)) * 5 + k] = v[k];
+  }
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence();
+    last = (atomicAdd(s.ticket, (unsigned)mine) == (unsigned)(ngroups - mine)) ? 1u : 0u;
+  }
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (!last) return;
+  __threadfence();
+  double tot[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int b = lane; b < ngroups; b += 32)
+#pragma unroll
+    for (int k = 0; k < 5; k++) tot[k] += __ldcg(&s.partials[b * 5 + k]);
+#pragma unroll
+  for (int k = 0; k < 5; k++)
+    for (int o = 16; o > 0; o >>= 1) tot[k] += __shfl_down_sync(0xffffffffu, tot[k], o);
+  if (lane == 0) {
+    *s.ticket = 0u;
     double cur[4];
     currents_from_sums(s.nfru, p.nfru_scale, p.depf, tot, cur);
 #pragma unroll

@@ -7,20 +7,20 @@
 
 namespace gw {
 
-__global__ void __launch_bounds__(32) fru_stage4_kernel(DevState s, StageParams p) {
-  cleft::stage_body<double>(s, p, blockIdx.x, gridDim.x, s.out);
+__global__ void __launch_bounds__(kMaxStageWarps * 32) fru_stage4_kernel(DevState s, StageParams p) {
+  cleft::stage_body<double>(s, p, blockIdx.x, s.out);
 }
 
-cudaError_t launch_stage4(const DevState& s, const StageParams& p, cudaStream_t st) {
-  const int blocks = (s.nfru + 7) / 8;
-  fru_stage4_kernel<<<blocks, 32, 0, st>>>(s, p);
+cudaError_t launch_stage4(const DevState& s, const StageParams& p, int warps, cudaStream_t st) {
+  const int blocks = stage_blocks(s.nfru, warps);
+  fru_stage4_kernel<<<blocks, 32 * warps, 0, st>>>(s, p);
   return cudaGetLastError();
 }
 
-__global__ void __launch_bounds__(32) fru_stage4_batch_kernel(BatchArgs a) { cleft::batch_body<double>(a); }
+__global__ void __launch_bounds__(kMaxStageWarps * 32) fru_stage4_batch_kernel(BatchArgs a) { cleft::batch_body<double>(a); }
 
-cudaError_t launch_stage4_batch(const BatchArgs& a, int nblocks, cudaStream_t st) {
-  fru_stage4_batch_kernel<<<nblocks, 32, 0, st>>>(a);
+cudaError_t launch_stage4_batch(const BatchArgs& a, int nblocks, int warps, cudaStream_t st) {
+  fru_stage4_batch_kernel<<<nblocks, 32 * warps, 0, st>>>(a);
   return cudaGetLastError();
 }
 

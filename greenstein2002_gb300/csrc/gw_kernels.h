@@ -9,6 +9,10 @@ namespace gw {
 // SM sub-partitions of a GB300, so single-warp blocks spread them over all
 // 152 SMs instead of leaving SMs idle.
 constexpr int kStageThreads = 32;
+// Cleft-parallel stage kernels: 8 FRUs per warp, 1 .. kMaxStageWarps warps
+// per block (a launch-shape choice only: the results are the same bits).
+constexpr int kMaxStageWarps = 8;
+inline int stage_blocks(int nfru, int warps) { return ((nfru + 7) / 8 + warps - 1) / warps; }
 // out[] slot of the device error flag (substep limit hit)
 constexpr int kOutError = 31;
 
@@ -25,7 +29,8 @@ enum : int { kSeedBase = 0, kSeedReference = 1 };
 //   mti[stride], mt[nfru][640] (FRU-major MT19937 rows)
 //   *_s               snapshot taken at the last save
 //   mt_hold/hold_epoch  copy-on-twist protection of the saved MT words
-//   partials[nblocks][16], ticket: scratch of the deterministic grid reduction
+//   partials[max(nblocks, ceil(nfru/8))][16], ticket: scratch of the
+//                     deterministic grid reduction
 //   out[32]           [0..4] flux sums, [5..8] Jxfer,Jtr,ICa,Ito2, [16..26] averages,
 //                     [31] error flag
 struct DevState {
@@ -43,6 +48,10 @@ struct DevState {
   unsigned* ticket;
   double* out;
   unsigned long long* substeps;
+  // stage trace (null unless enabled): substeps of every FRU in the last
+  // 4-lane launch, and each 8-FRU warp's begin/end global time (ns)
+  uint32_t* trace_sub;
+  unsigned long long* trace_ns;
 };
 
 struct StageParams {
@@ -55,7 +64,7 @@ struct StageParams {
 };
 
 // Many cells in one launch (cleft-parallel kernels): cell i owns blocks
-// block0[i] .. block0[i+1]-1 (8 FRUs per block); params[i].flags < 0 means
+// block0[i] .. block0[i+1]-1 (8 FRUs per warp); params[i].flags < 0 means
 // the cell has no operation this round; its totals go to outs[i*32 ..] in the
 // layout of DevState::out.
 constexpr int kBatchOutStride = 32;
@@ -68,12 +77,13 @@ struct BatchArgs {
 };
 
 cudaError_t launch_stage(const DevState& s, const StageParams& p, cudaStream_t st);
-cudaError_t launch_stage4_batch(const BatchArgs& a, int nblocks, cudaStream_t st);
-cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, cudaStream_t st);
-// cleft-parallel variants: 4 lanes per FRU, 8 FRUs per single-warp block;
-// FP64 (the plain method) and mixed precision (FP32 rates and local ODE)
-cudaError_t launch_stage4(const DevState& s, const StageParams& p, cudaStream_t st);
-cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, cudaStream_t st);
+cudaError_t launch_stage4_batch(const BatchArgs& a, int nblocks, int warps, cudaStream_t st);
+cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, int warps, cudaStream_t st);
+// cleft-parallel variants: 4 lanes per FRU, 8 FRUs per warp, `warps` warps
+// per block; FP64 (the plain method) and mixed precision (FP32 rates and
+// local ODE)
+cudaError_t launch_stage4(const DevState& s, const StageParams& p, int warps, cudaStream_t st);
+cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, int warps, cudaStream_t st);
 cudaError_t launch_avg(const DevState& s, cudaStream_t st);
 // FP64 FMA throughput of the device (TFLOP/s, best of a few launches).
 cudaError_t probe_fp64(int sms, double* tflops);

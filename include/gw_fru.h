@@ -88,6 +88,9 @@ int gw_resume(gw_ctx *ctx);
  * 8 FRUs per warp, shortest FP64 chain per FRU; 1 = one thread per FRU, 32
  * FRUs per warp.  Results are identical; the choice only changes speed. */
 int gw_set_fru_lanes(gw_ctx *ctx, int lanes);
+/* Warps per block of the 4-lane stage kernels: 1 (default), 2, 4 or 8.  A
+ * launch-shape choice only; every value gives the same results. */
+int gw_set_stage_warps(gw_ctx *ctx, int warps);
 
 /* Arithmetic of the FRU path: 0 (default) = FP64, the plain method;
  * 1 = mixed precision: transition rates and the FRU-local Ca ODE in FP32,
@@ -110,6 +113,14 @@ int gw_sync(gw_ctx *ctx);
 int gw_event_record(gw_ctx *ctx, int slot);
 int gw_event_elapsed(gw_ctx *ctx, int slot_a, int slot_b, float *ms);
 int gw_profile(gw_ctx *ctx, int enable);
+/* Stage trace (diagnostics of the 4-lane kernels; no reference
+ * counterpart): when enabled, every stage launch records each FRU's substep
+ * count and each 8-FRU warp's begin and end global time in ns;
+ * gw_stage_trace_read returns the last launch's: substeps[nfru],
+ * warp_ns[ceil(nfru/8)][2] (either may be NULL).  Enable before the cell
+ * joins a batch. */
+int gw_stage_trace(gw_ctx *ctx, int enable);
+int gw_stage_trace_read(gw_ctx *ctx, uint32_t *substeps, unsigned long long *warp_ns);
 int gw_profile_read(gw_ctx *ctx, double *stage_kernel_ms, unsigned long long *stage_launches);
 int gw_launches(gw_ctx *ctx, unsigned long long *count);
 int gw_l2_flush(gw_ctx *ctx);
@@ -202,6 +213,22 @@ int gw_batch_run(gw_batch *batch, int n, gw_ctx **cells, const gw_settings *sets
  * thread, its kernels running concurrently with the others'. */
 int gw_run_concurrent(int n, gw_ctx **cells, const gw_settings *sets, double *t, double *states, double *oldsteps,
                       int n_steps, double *state_trace, double *other_trace);
+/* Warps per block of the batch's launches (1, 2, 4 or 8; same results). */
+int gw_batch_set_warps(gw_batch *batch, int warps);
+
+/* Autotuner (no reference counterpart): runs window_ms of the cells' own
+ * workload from their current state once per stage-kernel launch shape --
+ * 4 lanes per FRU with 1, 2, 4 or 8 warps per block, and 1 lane per FRU
+ * (FP64 cells with the reference PCa, not in a batch) -- then restores
+ * their state and sets the fastest shape on every cell (and on the batch).
+ * The cells run alone (n = 1), concurrently on their own streams (batch
+ * NULL) or through the batch.  t, states [n][37] and oldsteps are read, not
+ * advanced.  ms (may be NULL) receives the wall time of each of the
+ * GW_TUNE_CANDIDATES candidates in the order above, -1 where not run.
+ * Results never depend on the shape chosen. */
+#define GW_TUNE_CANDIDATES 5
+int gw_autotune(int n, gw_ctx **cells, const gw_settings *sets, const double *t, const double *states,
+                const double *oldsteps, double window_ms, gw_batch *batch, int *lanes, int *warps, double *ms);
 
 /* ------------------------------------------------------------------------- */
 /* Serving: requests arrive at any time and run concurrently through one     */
