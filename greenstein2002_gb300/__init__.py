@@ -132,6 +132,7 @@ def bind(path):
         "gw_launches": ([vp, P(C.c_ulonglong)], C.c_int),
         "gw_l2_flush": ([vp], C.c_int),
         "gw_probe_fp64_peak": ([P(C.c_double)], C.c_int),
+        "gw_probe_fcn": ([P(C.c_double), P(C.c_double)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name, None)
@@ -314,6 +315,14 @@ class Cell:
                              _ptr(cu)), "gw_run", self._L)
         self.oldstep = os_.value
         return tt.value, st, ot, cu
+
+
+def fcn_cost_us(lib=None):
+    """(device us, host us) per evaluation of the global right-hand side."""
+    L = lib if lib is not None else load()
+    d, h = C.c_double(0.0), C.c_double(0.0)
+    _check(L.gw_probe_fcn(C.byref(d), C.byref(h)), "gw_probe_fcn", L)
+    return d.value, h.value
 
 
 def fp64_peak_tflops():

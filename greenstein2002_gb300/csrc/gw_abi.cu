@@ -489,6 +489,12 @@ extern "C" int gw_l2_flush(gw_ctx* c) {
   return GW_OK;
 }
 
+extern "C" int gw_probe_fcn(double* device_us, double* host_us) {
+  if (!device_us || !host_us) return set_err(GW_EINVAL, "gw_probe_fcn: null argument");
+  CK(gw::probe_fcn(device_us, host_us));
+  return GW_OK;
+}
+
 extern "C" int gw_probe_fp64_peak(double* tflops) {
   if (!tflops) return set_err(GW_EINVAL, "gw_probe_fp64_peak: null argument");
   int dev = 0, sms = 0;

@@ -179,12 +179,10 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
     else V = P->vclamp_hold;
   }
   /* ---- clamp with a prepulse, fcn.c:485-516 ---- */
-  double t_vpp_on = 0.0;
   if (P->vppclamp_flag) {
     const double on = floor((time - P->vppclamp_shift) / P->vppclamp_period) * P->vppclamp_period;
     const double ppoff = on + P->vppclamp_ppduration;
     const double off = on + P->vppclamp_duration + P->vppclamp_ppduration;
-    t_vpp_on = on;
     if (((time - P->vppclamp_shift) >= on) && (on >= 0.0) && ((time - P->vppclamp_shift) < ppoff)) {
       V = P->vppclamp_ppset;
     } else if (((time - P->vppclamp_shift) >= ppoff) && (on >= 0.0) && ((time - P->vppclamp_shift) < off)) {
@@ -367,7 +365,6 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
     dV = -Itot;
   }
   if (P->vppclamp_flag) {
-    (void)t_vpp_on;
     dV = 0.0;
     state[GW_V] = V;
     Itot = a1 + a2 + a3;

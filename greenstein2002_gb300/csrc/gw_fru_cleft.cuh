@@ -156,69 +156,102 @@ __device__ __forceinline__ R gmax(const Group& g, R v) {
   return v;
 }
 
-// Cooperative in-place regeneration of an FRU's 624 words by its 4 lanes, in
-// chunks of 4 consecutive words.  Words k >= 227 depend on words the same
-// regeneration produced 227 positions earlier (other lanes), so the group
-// synchronises after every chunk.
-__device__ __forceinline__ void regen4(uint32_t* m, const Group& g) {
-  for (int k0 = 0; k0 < kMtN; k0 += 4) {
-    const int k = k0 + g.c;
-    const uint32_t cur = m[k];
-    const uint32_t nxt = m[(k + 1 == kMtN) ? 0 : k + 1];
-    const uint32_t far = m[(k + kMtM) % kMtN];
-    __syncwarp(g.mask);
-    const uint32_t y = (cur & 0x80000000u) | (nxt & 0x7fffffffu);
-    m[k] = far ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
-    __syncwarp(g.mask);
+// In-place regeneration of one FRU's 624 words (mt19937_local.c:97-154) by
+// all 32 lanes of the warp, 32 consecutive words per step.  Word k < 227
+// reads the old word k + 397 (not reached yet), word k >= 227 the new word
+// k - 227 (written at least seven steps earlier) and word 623 the new words 0
+// and 396, as in the sequential loop; every lane reads before the barrier
+// and writes after it.
+__device__ __forceinline__ void regen32(uint32_t* m, int lane) {
+  for (int k0 = 0; k0 < kMtN; k0 += 32) {
+    const int k = k0 + lane;
+    const bool in = k < kMtN;
+    uint32_t nw = 0u;
+    if (in) {
+      const uint32_t cur = m[k];
+      const uint32_t nxt = m[(k + 1 == kMtN) ? 0 : k + 1];
+      const uint32_t far = m[(k + kMtM < kMtN) ? k + kMtM : k + kMtM - kMtN];
+      const uint32_t y = (cur & 0x80000000u) | (nxt & 0x7fffffffu);
+      nw = far ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+    }
+    __syncwarp();
+    if (in) m[k] = nw;
+    __syncwarp();
   }
 }
 __device__ __forceinline__ void copy4(uint32_t* dst, const uint32_t* src, const Group& g) {
   for (int k = g.c; k < kMtN; k += 4) dst[k] = src[k];
   __syncwarp(g.mask);
 }
+// 624 words in 16-byte pieces by the group's 4 lanes (rows 16-byte aligned)
+__device__ __forceinline__ void copy_row16(uint32_t* dst, const uint32_t* src, const Group& g) {
+  const uint4* s4 = reinterpret_cast<const uint4*>(src);
+  uint4* d4 = reinterpret_cast<uint4*>(dst);
+  for (int i = g.c; i < kMtN / 4; i += 4) d4[i] = s4[i];
+  __syncwarp(g.mask);
+}
 
+// The launch's view of one warp's 8 FRUs: their MT rows staged in shared
+// memory, and the global copy-on-twist rows of the first of them.
 struct StageCtx {
   const StageParams* p;
-  uint32_t* m;          // MT row of this FRU
-  uint32_t* hold;       // copy-on-twist row
-  uint32_t* hold_epoch;
+  uint32_t* rows;         // 8 shared-memory rows, kMtSmemStride words apart
+  uint32_t* m;            // this lane's FRU row (one of rows)
+  uint32_t* hold0;        // copy-on-twist rows (global), FRU-major, of the warp's FRUs
+  uint32_t* hold_epoch0;  // their epochs
+  bool dirty;             // this FRU's staged words differ from its global row
 };
 
-// Fetch the words of one substep: E_tot extra draws (lane c owns positions
-// pre .. pre+ne-1) followed by the 32 batch draws (lane c owns 8c .. 8c+7),
-// regenerating the row in between when the stream crosses word 624.
-__device__ __forceinline__ void fetch_words(const StageCtx& sc, const Group& g, int& mti, int pre, int ne, int etot,
-                                            uint32_t ex[kRyR], uint32_t bw[8]) {
-  const int W = etot + 32;
-  const bool cross = (mti + W > kMtN);
-  int pos;
-  // old generation first
+// The words of one substep are E_tot extra draws (lane c owns positions
+// pre .. pre+ne-1) followed by the 32 batch draws (lane c owns 8c .. 8c+7).
+// fetch_old reads those below word 624; regen_crossing then regenerates, with
+// the whole warp, the rows whose draws run past it; fetch_new reads the rest
+// from the new generation, tempers, and advances mti.
+__device__ __forceinline__ void fetch_old(const StageCtx& sc, const Group& g, int mti, int pre, int ne, int etot,
+                                          uint32_t ex[kRyR], uint32_t bw[8]) {
 #pragma unroll
   for (int i = 0; i < kRyR; i++) {
-    pos = mti + pre + i;
+    const int pos = mti + pre + i;
     if (i < ne && pos < kMtN) ex[i] = sc.m[pos];
   }
 #pragma unroll
   for (int k = 0; k < 8; k++) {
-    pos = mti + etot + 8 * g.c + k;
+    const int pos = mti + etot + 8 * g.c + k;
     if (pos < kMtN) bw[k] = sc.m[pos];
   }
-  if (cross) {
-    const bool need_copy = *sc.hold_epoch != sc.p->epoch;
-    __syncwarp(g.mask);  // every lane has read its old words and the epoch
-    if (need_copy) {
-      copy4(sc.hold, sc.m, g);
-      if (g.c == 0) *sc.hold_epoch = sc.p->epoch;
+}
+
+// cross / copy: bit 4*i set when group i regenerates / first copies its
+// pre-regeneration words to its hold row in this epoch (lane 4*i's ballot).
+__device__ __forceinline__ void regen_crossing(const StageCtx& sc, int lane, unsigned cross, unsigned copy) {
+  while (cross) {
+    const int l0 = __ffs(cross) - 1;
+    cross &= cross - 1u;
+    const int gi = l0 >> 2;
+    uint32_t* row = sc.rows + gi * kMtSmemStride;
+    __syncwarp();  // group gi has read its old words
+    if (copy & (1u << l0)) {
+      const uint4* s4 = reinterpret_cast<const uint4*>(row);
+      uint4* d4 = reinterpret_cast<uint4*>(sc.hold0 + (size_t)gi * kMtStride);
+      for (int i = lane; i < kMtN / 4; i += 32) d4[i] = s4[i];
+      if (lane == 0) sc.hold_epoch0[gi] = sc.p->epoch;
     }
-    regen4(sc.m, g);
+    regen32(row, lane);
+  }
+}
+
+__device__ __forceinline__ void fetch_new(const StageCtx& sc, const Group& g, int& mti, int pre, int ne, int etot,
+                                          uint32_t ex[kRyR], uint32_t bw[8]) {
+  const int W = etot + 32;
+  if (mti + W > kMtN) {
 #pragma unroll
     for (int i = 0; i < kRyR; i++) {
-      pos = mti + pre + i;
+      const int pos = mti + pre + i;
       if (i < ne && pos >= kMtN) ex[i] = sc.m[pos - kMtN];
     }
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-      pos = mti + etot + 8 * g.c + k;
+      const int pos = mti + etot + 8 * g.c + k;
       if (pos >= kMtN) bw[k] = sc.m[pos - kMtN];
     }
     mti = mti + W - kMtN;
@@ -278,9 +311,10 @@ __device__ __forceinline__ float frac_of(double t, double t0, double, float rint
 }
 
 // One FRU over [t0, tf] by its four lanes (simfru_local.c:83-277).  cajsr and
-// cass are the FRU's FP64 state; arithmetic runs in R.
+// cass are the FRU's FP64 state; arithmetic runs in R.  Every lane of the
+// warp calls it together (live = false for a group without an FRU).
 template <typename R>
-__device__ __forceinline__ void advance4(const StageCtx& sc, const Group& g, double& cajsr64, double& cass64,
+__device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live, double& cajsr64, double& cass64,
                                          uint32_t& w, int& mti, uint32_t& nsub, bool& overflow) {
   const StageParams& p = *sc.p;
   R dep0[3], span[3], dep[3];
@@ -309,177 +343,201 @@ __device__ __forceinline__ void advance4(const StageCtx& sc, const Group& g, dou
   const R cCF = isdiv ? R(0.0) : (g.c == 0 ? R(alphacf) : R(betacf));
   const R cK = isdiv ? (g.c == 2 ? R(0.4) : R(340.0)) : R(1.0);
   const R cM = isdiv ? (g.c == 2 ? R(1.0 - 0.4) : R(60.0)) : R(0.0);
+  const int lane = threadIdx.x & 31;
   while (true) {
-    // the loop condition is uniform over the group (t is the same in all four lanes)
-    if (!(t < p.tf)) break;
-    if (nsub >= (1u << 22)) {
+    // all 32 lanes stay in the loop until every FRU of the warp is done, so
+    // the warp can regenerate MT rows together; a group whose FRU has
+    // reached tf (or never had one) idles
+    bool go = live && t < p.tf;
+    if (go && nsub >= (1u << 22)) {
       overflow = true;
-      break;
+      go = false;
     }
-    const R cajsr = (R)cajsr64, cass = (R)cass64;
-    // ---- voltage terms at the substep start, one exponential per lane ----
-    const R x = dep[0] + cA;
-    R q = x * cR;
-    if (isdiv) q = divc(x, cD, cR);
-    const R ev = rexp(q);
-    const R r01 = cCF * ev;
-    const R r23 = rdiv(cK, R(1) + ev) + cM;
-    const R vterm = isdiv ? r23 : r01;
-    const R alpha = from(g, vterm, 0), beta = from(g, vterm, 1);
-    const R yinf = from(g, vterm, 2), tau = from(g, vterm, 3);
-    const R bp = divc(beta, R(bL * kappa), R(1.0 / (bL * kappa)));
-    const R ap = R(aL) * alpha;
-    // ---- exit totals of this cleft's 8 channels ----
-    const R gam = R(gammacf) * cass;
+    if (!__any_sync(0xffffffffu, go)) break;
+    R cajsr = R(0), cass = R(0), alpha = R(0), beta = R(0), bp = R(0), gam = R(0);
+    R k12 = R(0), k23 = R(0), k34 = R(0), k54 = R(0), k25 = R(0), k56 = R(0);
     R R0[8];
-    {
-      const int s = lcc_of(w);
-      const uint16_t bi = c_lcc_basis[s];
-      const R X = R(c_lcc_coef[s][0]) * pick_basis(bi & 15, alpha, beta, gam, ap, bp);
-      const R Y = R(c_lcc_coef[s][1]) * pick_basis((bi >> 4) & 15, alpha, beta, gam, ap, bp);
-      const R Z = R(c_lcc_coef[s][2]) * pick_basis((bi >> 8) & 15, alpha, beta, gam, ap, bp);
-      R0[0] = X + Y + Z;
-    }
-    {
-      const R num = (vdi_of(w) == 2) ? (R(1) - yinf) : yinf;
-      R0[1] = rdiv(num, tau);
-    }
-    // RyR constants of the cleft and the pseudo-state draws
-    const R c2 = cass * cass;
-    const R sat = imin(R(threshMAX), divc(c2, R(k_rate), R(1.0 / k_rate)));
-    const R sat2 = imin(R(threshMAX), divc(c2, R(k_rate2), R(1.0 / k_rate2)));
-    const R k12 = R(k12cf) * sat2, k23 = R(k23cf) * sat, k34 = R(k34cf) * sat;
-    const R k54 = R(k54cf) * sat, k25 = R(k25cf) * sat, k56 = R(k56cf) * sat;
-    int regime;
-    {
-      const R cc = imin(cass, R(threshMAXCa));
-      regime = ilt(cc, R(threshCa56to8)) ? 0 : (ilt(cc, R(threshCa34to7)) ? 1 : 2);
-    }
-    // extra draws: regime 0 resolves 7 and 8, regime 1 resolves 7 (in cleft, then RyR order)
-    int ne = 0;
-#pragma unroll
-    for (int i = 0; i < kRyR; i++) {
-      const int s = ryr_of(w, i);
-      ne += (regime == 0 && (s == 7 || s == 8)) || (regime == 1 && s == 7);
-    }
-    const int n0 = from(g, ne, 0), n1 = from(g, ne, 1), n2 = from(g, ne, 2), n3 = from(g, ne, 3);
-    const int pre = (g.c > 0 ? n0 : 0) + (g.c > 1 ? n1 : 0) + (g.c > 2 ? n2 : 0);
-    const int etot = n0 + n1 + n2 + n3;
+    int regime = 0, ne = 0, pre = 0, etot = 0;
     uint32_t exw[kRyR] = {0u, 0u, 0u, 0u, 0u}, bw[8];
-    fetch_words(sc, g, mti, pre, ne, etot, exw, bw);
-    {
-      int used = 0;
-#pragma unroll
+    if (go) {
+      cajsr = (R)cajsr64;
+      cass = (R)cass64;
+      // ---- voltage terms at the substep start, one exponential per lane ----
+      const R x = dep[0] + cA;
+      R q = x * cR;
+      if (isdiv) q = divc(x, cD, cR);
+      const R ev = rexp(q);
+      const R r01 = cCF * ev;
+      const R r23 = rdiv(cK, R(1) + ev) + cM;
+      const R vterm = isdiv ? r23 : r01;
+      alpha = from(g, vterm, 0);
+      beta = from(g, vterm, 1);
+      const R yinf = from(g, vterm, 2), tau = from(g, vterm, 3);
+      bp = divc(beta, R(bL * kappa), R(1.0 / (bL * kappa)));
+      const R ap = R(aL) * alpha;
+      // ---- exit totals of this cleft's 8 channels ----
+      gam = R(gammacf) * cass;
+      {
+        const int s = lcc_of(w);
+        const uint16_t bi = c_lcc_basis[s];
+        const R X = R(c_lcc_coef[s][0]) * pick_basis(bi & 15, alpha, beta, gam, ap, bp);
+        const R Y = R(c_lcc_coef[s][1]) * pick_basis((bi >> 4) & 15, alpha, beta, gam, ap, bp);
+        const R Z = R(c_lcc_coef[s][2]) * pick_basis((bi >> 8) & 15, alpha, beta, gam, ap, bp);
+        R0[0] = X + Y + Z;
+      }
+      {
+        const R num = (vdi_of(w) == 2) ? (R(1) - yinf) : yinf;
+        R0[1] = rdiv(num, tau);
+      }
+      // RyR constants of the cleft and the pseudo-state draws
+      const R c2 = cass * cass;
+      const R sat = imin(R(threshMAX), divc(c2, R(k_rate), R(1.0 / k_rate)));
+      const R sat2 = imin(R(threshMAX), divc(c2, R(k_rate2), R(1.0 / k_rate2)));
+      k12 = R(k12cf) * sat2;
+      k23 = R(k23cf) * sat;
+      k34 = R(k34cf) * sat;
+      k54 = R(k54cf) * sat;
+      k25 = R(k25cf) * sat;
+      k56 = R(k56cf) * sat;
+      {
+        const R cc = imin(cass, R(threshMAXCa));
+        regime = ilt(cc, R(threshCa56to8)) ? 0 : (ilt(cc, R(threshCa34to7)) ? 1 : 2);
+      }
+      // extra draws: regime 0 resolves 7 and 8, regime 1 resolves 7 (in cleft, then RyR order)
+      ne = 0;
+  #pragma unroll
       for (int i = 0; i < kRyR; i++) {
-        int s = ryr_of(w, i);
-        if (regime == 0) {
-          if (s == 7 || s == 8) {
-            const double u = (double)exw[used++] / 4294967296.0;
-            if (s == 7) s = (u < (double)(k34 / (k34 + R(k43)))) ? 4 : 3;
-            else s = (u < (double)(k56 / (k56 + R(k65)))) ? 6 : 5;
+        const int s = ryr_of(w, i);
+        ne += (regime == 0 && (s == 7 || s == 8)) || (regime == 1 && s == 7);
+      }
+      const int n0 = from(g, ne, 0), n1 = from(g, ne, 1), n2 = from(g, ne, 2), n3 = from(g, ne, 3);
+      pre = (g.c > 0 ? n0 : 0) + (g.c > 1 ? n1 : 0) + (g.c > 2 ? n2 : 0);
+      etot = n0 + n1 + n2 + n3;
+      fetch_old(sc, g, mti, pre, ne, etot, exw, bw);
+    }
+    // rows whose draws run past word 624 are regenerated by the whole warp
+    const bool cross = go && (mti + etot + 32 > kMtN);
+    const unsigned cross_mask = __ballot_sync(0xffffffffu, cross && g.c == 0);
+    const unsigned copy_mask =
+        __ballot_sync(0xffffffffu, cross && g.c == 0 && sc.hold_epoch0[lane >> 2] != p.epoch);
+    if (cross_mask) regen_crossing(sc, lane, cross_mask, copy_mask);
+    if (cross) sc.dirty = true;
+    if (go) {
+      fetch_new(sc, g, mti, pre, ne, etot, exw, bw);
+      {
+        int used = 0;
+  #pragma unroll
+        for (int i = 0; i < kRyR; i++) {
+          int s = ryr_of(w, i);
+          if (regime == 0) {
+            if (s == 7 || s == 8) {
+              const double u = (double)exw[used++] / 4294967296.0;
+              if (s == 7) s = (u < (double)(k34 / (k34 + R(k43)))) ? 4 : 3;
+              else s = (u < (double)(k56 / (k56 + R(k65)))) ? 6 : 5;
+            }
+          } else if (regime == 1) {
+            if (s == 7) {
+              const double u = (double)exw[used++] / 4294967296.0;
+              s = (u < (double)(k34 / (k34 + R(k43)))) ? 4 : 3;
+            }
+            if (s == 5 || s == 6) s = 8;
+          } else {
+            if (s == 3 || s == 4) s = 7;
+            else if (s == 5 || s == 6) s = 8;
           }
-        } else if (regime == 1) {
-          if (s == 7) {
-            const double u = (double)exw[used++] / 4294967296.0;
-            s = (u < (double)(k34 / (k34 + R(k43)))) ? 4 : 3;
-          }
-          if (s == 5 || s == 6) s = 8;
-        } else {
-          if (s == 3 || s == 4) s = 7;
-          else if (s == 5 || s == 6) s = 8;
+          w = set_field(w, 8 + 4 * i, s);
         }
-        w = set_field(w, 8 + 4 * i, s);
       }
-    }
-    {
-      bool need7 = false, need8 = false;
-#pragma unroll
-      for (int i = 0; i < kRyR; i++) {
-        const int s = ryr_of(w, i);
-        need7 |= (s == 7);
-        need8 |= (s == 8);
+      {
+        bool need7 = false, need8 = false;
+  #pragma unroll
+        for (int i = 0; i < kRyR; i++) {
+          const int s = ryr_of(w, i);
+          need7 |= (s == 7);
+          need8 |= (s == 8);
+        }
+        const R T2 = R(k21) + k23 + k25, T3 = R(k32) + k34, T5 = R(k52) + k54 + k56;
+        const R T4 = R(k43 + k45);
+        R T7 = R(0), T8 = R(0);
+        if (need7) {
+          const R a1 = k34 / (R(k43) + k34);
+          T7 = (R(1) - a1) * R(k32) + a1 * R(k45);
+        }
+        if (need8) {
+          const R a1 = R(k65) / (k56 + R(k65));
+          T8 = a1 * R(k52) + a1 * k54;
+        }
+  #pragma unroll
+        for (int i = 0; i < kRyR; i++) {
+          const int s = ryr_of(w, i);
+          R r = k12;
+          r = (s == 2) ? T2 : r;
+          r = (s == 3) ? T3 : r;
+          r = (s == 4) ? T4 : r;
+          r = (s == 5) ? T5 : r;
+          r = (s == 6) ? R(k65) : r;
+          r = (s == 7) ? T7 : r;
+          r = (s == 8) ? T8 : r;
+          R0[2 + i] = r;
+        }
       }
-      const R T2 = R(k21) + k23 + k25, T3 = R(k32) + k34, T5 = R(k52) + k54 + k56;
-      const R T4 = R(k43 + k45);
-      R T7 = R(0), T8 = R(0);
-      if (need7) {
-        const R a1 = k34 / (R(k43) + k34);
-        T7 = (R(1) - a1) * R(k32) + a1 * R(k45);
-      }
-      if (need8) {
-        const R a1 = R(k65) / (k56 + R(k65));
-        T8 = a1 * R(k52) + a1 * k54;
-      }
-#pragma unroll
-      for (int i = 0; i < kRyR; i++) {
-        const int s = ryr_of(w, i);
-        R r = k12;
-        r = (s == 2) ? T2 : r;
-        r = (s == 3) ? T3 : r;
-        r = (s == 4) ? T4 : r;
-        r = (s == 5) ? T5 : r;
-        r = (s == 6) ? R(k65) : r;
-        r = (s == 7) ? T7 : r;
-        r = (s == 8) ? T8 : r;
-        R0[2 + i] = r;
-      }
-    }
-    R0[7] = (cl_of(w) == 1) ? R(kfIto2) * cass : R(kbIto2);
-    R mx = R(0);
-#pragma unroll
-    for (int j = 0; j < 8; j++) mx = imax(mx, R0[j]);
-    mx = gmax(g, mx);
-    // ---- substep size (simfru_local.c:135-146) ----
-    R dtr = imin(rdiv(R(0.1), mx), R(10.001e-3));
-    const R cmax = gmax(g, imax(R(0.e-3), cass));
-    if (cmax > R(1.5e-3)) dtr = imin(dtr, R(5.001e-3));
-    const double dt64 = imin((double)dtr, p.tf - t);
-    const R dt = (R)dt64;
-    // ---- Heun step (simfru_local.c:149-173) ----
-    R dJ, dS;
-    fcn_fru4(g, cajsr, cass, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
-    const R k1J = dt * dJ, k1S = dt * dS;
-    const R y1J = cajsr + k1J, y1S = cass + k1S;
-    t = t + dt64;
-    const R frac = frac_of(t, p.t0, interval, rinterval);
-#pragma unroll
-    for (int i = 0; i < 3; i++) dep[i] = dep0[i] + frac * span[i];
-    ghk_terms(dep[0], pca_scale, e2, a2j, small);
-    fcn_fru4(g, y1J, y1S, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
-    cajsr64 = cajsr64 + (double)((k1J + dt * dJ) / R(2));
-    cass64 = cass64 + (double)((k1S + dt * dS) / R(2));
-    // ---- transitions of this cleft's 8 channels (:215-276) ----
-    bool moved = false;
-    if (leave_gt(bw[0], dt, R0[0])) {
-      const LccBasis lb{(double)alpha, (double)beta, (double)bp};
-      double r[4];
-      int d[4];
-      const int len = lcc_row(lcc_of(w), lb, (double)gam, r, d);
-      w = set_field(w, 0, pick_dest(r, d, len, (double)dt, (double)bw[0] / 4294967296.0));
-    }
-    if (leave_ge(bw[1], dt, R0[1])) w = set_field(w, 4, 3 - vdi_of(w));
-#pragma unroll
-    for (int i = 0; i < kRyR; i++) {
-      if (leave_gt(bw[2 + i], dt, R0[2 + i])) {
-        RyrK k;
-        k.k12 = k12;
-        k.k23 = k23;
-        k.k34 = k34;
-        k.k54 = k54;
-        k.k25 = k25;
-        k.k56 = k56;
-        k.regime = regime;
+      R0[7] = (cl_of(w) == 1) ? R(kfIto2) * cass : R(kbIto2);
+      R mx = R(0);
+  #pragma unroll
+      for (int j = 0; j < 8; j++) mx = imax(mx, R0[j]);
+      mx = gmax(g, mx);
+      // ---- substep size (simfru_local.c:135-146) ----
+      R dtr = imin(rdiv(R(0.1), mx), R(10.001e-3));
+      const R cmax = gmax(g, imax(R(0.e-3), cass));
+      if (cmax > R(1.5e-3)) dtr = imin(dtr, R(5.001e-3));
+      const double dt64 = imin((double)dtr, p.tf - t);
+      const R dt = (R)dt64;
+      // ---- Heun step (simfru_local.c:149-173) ----
+      R dJ, dS;
+      fcn_fru4(g, cajsr, cass, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
+      const R k1J = dt * dJ, k1S = dt * dS;
+      const R y1J = cajsr + k1J, y1S = cass + k1S;
+      t = t + dt64;
+      const R frac = frac_of(t, p.t0, interval, rinterval);
+  #pragma unroll
+      for (int i = 0; i < 3; i++) dep[i] = dep0[i] + frac * span[i];
+      ghk_terms(dep[0], pca_scale, e2, a2j, small);
+      fcn_fru4(g, y1J, y1S, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
+      cajsr64 = cajsr64 + (double)((k1J + dt * dJ) / R(2));
+      cass64 = cass64 + (double)((k1S + dt * dS) / R(2));
+      // ---- transitions of this cleft's 8 channels (:215-276) ----
+      bool moved = false;
+      if (leave_gt(bw[0], dt, R0[0])) {
+        const LccBasis lb{(double)alpha, (double)beta, (double)bp};
         double r[4];
         int d[4];
-        const int len = ryr_row(ryr_of(w, i), k, r, d);
-        w = set_field(w, 8 + 4 * i, pick_dest(r, d, len, (double)dt, (double)bw[2 + i] / 4294967296.0));
-        moved = true;
+        const int len = lcc_row(lcc_of(w), lb, (double)gam, r, d);
+        w = set_field(w, 0, pick_dest(r, d, len, (double)dt, (double)bw[0] / 4294967296.0));
       }
+      if (leave_ge(bw[1], dt, R0[1])) w = set_field(w, 4, 3 - vdi_of(w));
+  #pragma unroll
+      for (int i = 0; i < kRyR; i++) {
+        if (leave_gt(bw[2 + i], dt, R0[2 + i])) {
+          RyrK k;
+          k.k12 = k12;
+          k.k23 = k23;
+          k.k34 = k34;
+          k.k54 = k54;
+          k.k25 = k25;
+          k.k56 = k56;
+          k.regime = regime;
+          double r[4];
+          int d[4];
+          const int len = ryr_row(ryr_of(w, i), k, r, d);
+          w = set_field(w, 8 + 4 * i, pick_dest(r, d, len, (double)dt, (double)bw[2 + i] / 4294967296.0));
+          moved = true;
+        }
+      }
+      if (leave_ge(bw[7], dt, R0[7])) w = set_field(w, 28, 3 - cl_of(w));
+      lopen = lcc_open(w) ? R(1) : R(0);
+      if (moved) nopen = ryr_open_count(w);
+      nsub++;
     }
-    if (leave_ge(bw[7], dt, R0[7])) w = set_field(w, 28, 3 - cl_of(w));
-    lopen = lcc_open(w) ? R(1) : R(0);
-    if (moved) nopen = ryr_open_count(w);
-    nsub++;
   }
 }
 
@@ -538,6 +596,7 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 template <typename R>
 __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, int bidx, double* out) {
+  extern __shared__ __align__(16) uint32_t mt_stage[];  // [warps][8][kMtSmemStride]
   const int lane = threadIdx.x & 31;
   const int grp = bidx * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
   const int ngroups = (s.nfru + 7) >> 3;
@@ -552,22 +611,26 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, in
   uint32_t nsub = 0;
   bool overflow = false;
   const bool active = f < s.nfru;  // uniform over each 4-lane group
+  const size_t nf = (size_t)s.stride;
+  double cajsr = 0.0, cass = 0.0;
+  uint32_t w = 0u;
+  int mti = 0;
+  uint32_t* gm = s.mt + (size_t)f * kMtStride;
+  StageCtx sc;
+  sc.p = &p;
+  sc.rows = mt_stage + (threadIdx.x >> 5) * 8 * kMtSmemStride;
+  sc.m = sc.rows + (lane >> 2) * kMtSmemStride;
+  sc.hold0 = s.mt_hold + (size_t)grp * 8 * kMtStride;
+  sc.hold_epoch0 = s.hold_epoch + grp * 8;
+  sc.dirty = false;
+  bool restore = false;
   if (active) {
-    const size_t nf = (size_t)s.stride;
-    double cajsr, cass;
-    uint32_t w;
-    int mti;
-    StageCtx sc;
-    sc.p = &p;
-    sc.m = s.mt + (size_t)f * kMtStride;
-    sc.hold = s.mt_hold + (size_t)f * kMtStride;
-    sc.hold_epoch = s.hold_epoch + f;
     if (p.flags & kFlagResume) {
       cajsr = s.frus_s[f];
       cass = s.frus_s[(g.c + 1) * nf + f];
       w = s.chan_s[g.c * nf + f];
       mti = s.mti_s[f];
-      if (*sc.hold_epoch == p.epoch) copy4(sc.m, sc.hold, g);
+      restore = (sc.hold_epoch0[lane >> 2] == p.epoch);
     } else {
       cajsr = s.frus[f];
       cass = s.frus[(g.c + 1) * nf + f];
@@ -582,7 +645,21 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, in
       s.frus_s[(g.c + 1) * nf + f] = cass;
       s.chan_s[g.c * nf + f] = w;
     }
-    if (p.flags & kFlagAdvance) advance4<R>(sc, g, cajsr, cass, w, mti, nsub, overflow);
+  }
+  const uint32_t* hold = sc.hold0 + (size_t)(lane >> 2) * kMtStride;
+  if (p.flags & kFlagAdvance) {
+    // the FRUs' MT rows live in shared memory for the whole launch: every
+    // draw and every regeneration is a shared-memory access
+    if (active) copy_row16(sc.m, restore ? hold : gm, g);
+    sc.dirty = restore;
+    __syncwarp();
+    advance4<R>(sc, g, active, cajsr, cass, w, mti, nsub, overflow);
+    __syncwarp();
+    if (active && sc.dirty) copy_row16(gm, sc.m, g);
+  } else if (active && restore) {
+    copy_row16(gm, hold, g);
+  }
+  if (active) {
     if (s.trace_sub && g.c == 0) s.trace_sub[f] = nsub;
     if (g.c == 0) {
       s.frus[f] = cajsr;

@@ -13,14 +13,18 @@ __global__ void __launch_bounds__(kMaxStageWarps * 32) fru_stage4_kernel(DevStat
 
 cudaError_t launch_stage4(const DevState& s, const StageParams& p, int warps, cudaStream_t st) {
   const int blocks = stage_blocks(s.nfru, warps);
-  fru_stage4_kernel<<<blocks, 32 * warps, 0, st>>>(s, p);
+  static const cudaError_t attr = stage_smem_attributes(fru_stage4_kernel);
+  if (attr != cudaSuccess) return attr;
+  fru_stage4_kernel<<<blocks, 32 * warps, warps * kStageSmemPerWarp, st>>>(s, p);
   return cudaGetLastError();
 }
 
 __global__ void __launch_bounds__(kMaxStageWarps * 32) fru_stage4_batch_kernel(BatchArgs a) { cleft::batch_body<double>(a); }
 
 cudaError_t launch_stage4_batch(const BatchArgs& a, int nblocks, int warps, cudaStream_t st) {
-  fru_stage4_batch_kernel<<<nblocks, 32 * warps, 0, st>>>(a);
+  static const cudaError_t attr = stage_smem_attributes(fru_stage4_batch_kernel);
+  if (attr != cudaSuccess) return attr;
+  fru_stage4_batch_kernel<<<nblocks, 32 * warps, warps * kStageSmemPerWarp, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -3,6 +3,9 @@
 // lists no FP64 figure, so the benchmark measures this denominator in-run.
 #include <cuda_runtime.h>
 
+#include <chrono>
+
+#include "gw_cell_model.h"
 #include "gw_kernels.h"
 
 namespace gw {
@@ -41,6 +44,59 @@ cudaError_t probe_fp64(int sms, double* tflops) {
   cudaEventDestroy(e1);
   cudaFree(out);
   *tflops = best;
+  return e;
+}
+
+// Cost of the global right-hand side (fcn.c:29-1072) on one GPU thread:
+// `calls` dependent evaluations at the rest state (each call's dV feeds the
+// next call's V by a negligible amount, so none can be skipped).
+__global__ void fcn_chain(const gw_protocol* P, int calls, double* out) {
+  double y[GW_NSTATE], F[GW_NSTATE], cur[GW_NCUR];
+  gw_rest_state(y);
+  for (int i = 0; i < calls; i++) {
+    gw_fcn(10.5, y, F, cur, 1, 1e-6, 1e-6, -1e-3, 0.0, P);
+    y[GW_V] = y[GW_V] + 1e-30 * F[GW_V];
+  }
+  out[0] = y[GW_V] + cur[GW_I_ICa];
+}
+
+cudaError_t probe_fcn(double* device_us, double* host_us) {
+  const int calls = 200;
+  gw_protocol hp;
+  gw_protocol_defaults(&hp);
+  gw_protocol* dp = nullptr;
+  double* out = nullptr;
+  cudaEvent_t e0, e1;
+  cudaError_t e = cudaMalloc(&dp, sizeof hp);
+  if (e == cudaSuccess) e = cudaMalloc(&out, sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpy(dp, &hp, sizeof hp, cudaMemcpyHostToDevice);
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {
+    cudaEventRecord(e0);
+    fcn_chain<<<1, 1>>>(dp, calls, out);
+    cudaEventRecord(e1);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && rep > 0) best = ms < best ? ms : best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(dp);
+  cudaFree(out);
+  *device_us = 1e3 * best / calls;
+  // the same chain on the host
+  double y[GW_NSTATE], F[GW_NSTATE], cur[GW_NCUR];
+  gw_rest_state(y);
+  const auto t0 = std::chrono::steady_clock::now();
+  for (int i = 0; i < 20 * calls; i++) {
+    gw_fcn(10.5, y, F, cur, 1, 1e-6, 1e-6, -1e-3, 0.0, &hp);
+    y[GW_V] = y[GW_V] + 1e-30 * F[GW_V];
+  }
+  const double us = std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
+  *host_us = us / (20 * calls) + 0.0 * (y[GW_V] + cur[GW_I_ICa]);
   return e;
 }
 

@@ -125,6 +125,10 @@ int gw_profile_read(gw_ctx *ctx, double *stage_kernel_ms, unsigned long long *st
 int gw_launches(gw_ctx *ctx, unsigned long long *count);
 int gw_l2_flush(gw_ctx *ctx);
 int gw_probe_fp64_peak(double *tflops);
+/* Microseconds per evaluation of the global right-hand side (fcn.c) on one
+ * GPU thread and on the host: what a device-resident integrator would pay
+ * per stage on GB300's FP64 rate. */
+int gw_probe_fcn(double *device_us, double *host_us);
 
 /* Allocation-free FRU stage (no counterpart in the reference).  For callers
  * that cannot allocate device memory while they run -- cudaMalloc
