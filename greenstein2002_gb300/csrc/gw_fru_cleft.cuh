@@ -51,6 +51,11 @@ template <typename R>
 __device__ __forceinline__ R imin(R a, R b) { return ord(a) < ord(b) ? a : b; }
 template <typename R>
 __device__ __forceinline__ bool ilt(R a, R b) { return ord(a) < ord(b); }
+// |v| < c for a positive constant c, on the integer pipe
+__device__ __forceinline__ bool abs_lt(double v, double c) {
+  return (__double_as_longlong(v) & 0x7fffffffffffffffLL) < __double_as_longlong(c);
+}
+__device__ __forceinline__ bool abs_lt(float v, float c) { return (__float_as_int(v) & 0x7fffffff) < __float_as_int(c); }
 
 // x / d for a compile-time constant d with r = 1/d: correctly rounded in FP64
 __device__ __forceinline__ double divc(double x, double d, double r) {
@@ -78,9 +83,10 @@ __device__ __forceinline__ void thresh(double P, uint64_t& fl, bool& exact) {
   }
 }
 // leaves its state when u > 1 - dt*R (LCC, RyR) ...
+__device__ __forceinline__ bool nonpos(double P) { return __double_as_longlong(P) <= 0LL; }  // P <= 0 (not NaN)
 __device__ __forceinline__ bool leave_gt(uint32_t y, double dt, double R) {
   const double P = 1.0 - dt * R;
-  if (P <= 0.0) return true;  // never on valid input (dt*rate <= 0.1)
+  if (nonpos(P)) return true;  // never on valid input (dt*rate <= 0.1)
   uint64_t fl;
   bool ex;
   thresh(P, fl, ex);
@@ -89,7 +95,7 @@ __device__ __forceinline__ bool leave_gt(uint32_t y, double dt, double R) {
 // ... or when u >= 1 - dt*R (VDI gate, Cl channel)
 __device__ __forceinline__ bool leave_ge(uint32_t y, double dt, double R) {
   const double P = 1.0 - dt * R;
-  if (P <= 0.0) return true;
+  if (nonpos(P)) return true;
   uint64_t fl;
   bool ex;
   thresh(P, fl, ex);
@@ -102,6 +108,35 @@ __device__ __forceinline__ bool leave_gt(uint32_t y, float dt, float R) {
 __device__ __forceinline__ bool leave_ge(uint32_t y, float dt, float R) {
   return (float)(4294967296ull - (uint64_t)y) <= dt * R * 4294967296.0f;
 }
+
+// Destination of a channel that leaves its state (simfru_local.c:215-253):
+// FP64 walks the reference's cumulative probabilities with u = y/2^32; FP32
+// walks the remaining exit mass against 1 - u = (2^32 - y)/2^32, which keeps
+// full resolution near u = 1 where the walk happens.
+__device__ __forceinline__ int choose_dest(const double r[4], const int d[4], int len, double dt, uint32_t y) {
+  return pick_dest(r, d, len, dt, (double)y / 4294967296.0);
+}
+__device__ __forceinline__ int choose_dest(const float r[4], const int d[4], int len, float dt, uint32_t y) {
+  const float c = (float)(4294967296ull - (uint64_t)y) * 2.3283064365386963e-10f;
+  float rem = dt * r[0] - dt * r[1];
+  int n = 1;
+  while (c < rem && n + 1 < len) {
+    n++;
+    rem = rem - dt * r[n];
+  }
+  return d[n];
+}
+
+// u = y/2^32 < p for 0 < p < 1 (pseudo-state draws, fru_rates_local.c):
+// FP64 in the integer domain (u < p <=> y < p*2^32); FP32 directly
+__device__ __forceinline__ bool u_below(uint32_t y, double p) {
+  if (nonpos(p)) return false;
+  uint64_t fl;
+  bool ex;
+  thresh(p, fl, ex);
+  return ex ? (uint64_t)y < fl : (uint64_t)y <= fl;
+}
+__device__ __forceinline__ bool u_below(uint32_t y, float p) { return (float)y * 2.3283064365386963e-10f < p; }
 
 // LCC exit total = (cX*bX + cY*bY) + cZ*bZ with bases {1, alpha, beta,
 // gamma, alpha', beta'}: the sums of fru_rates_local.c:176-340 in their order.
@@ -264,6 +299,19 @@ __device__ __forceinline__ void fetch_new(const StageCtx& sc, const Group& g, in
   for (int k = 0; k < 8; k++) bw[k] = mt_temper(bw[k]);
 }
 
+// JRyRmax * (R)n for n = 0..5 open RyRs, by selection instead of a
+// conversion and a multiply (the products are the same rounded values)
+template <typename R>
+__device__ __forceinline__ R jryr_coef(int n) {
+  R v = R(0);
+  v = (n == 1) ? R(JRyRmax) * R(1) : v;
+  v = (n == 2) ? R(JRyRmax) * R(2) : v;
+  v = (n == 3) ? R(JRyRmax) * R(3) : v;
+  v = (n == 4) ? R(JRyRmax) * R(4) : v;
+  v = (n == 5) ? R(JRyRmax) * R(5) : v;
+  return v;
+}
+
 // Local Ca ODE of one cleft (fcn_fru.c:23-137) evaluated by the FRU's four
 // lanes.  Each lane returns dCaSS of its cleft; every lane returns the same
 // dCaJSR.  e2 = exp(2 V F/RT) and a2j are passed in (shared by all lanes).
@@ -274,7 +322,7 @@ __device__ __forceinline__ void fcn_fru4(const Group& g, R cajsr, R cass, const 
   constexpr double KJDHsmall = -PCa * 2.0 * 1000.0 * Faraday;
   const R Cai = dep[1], CaNSR = dep[2];
   // JRyR of every cleft, summed in cleft order
-  const R jcoef = R(JRyRmax) * (R)nopen;
+  const R jcoef = jryr_coef<R>(nopen);
   const R JRyR = jcoef * (cajsr - cass);
   const R j0 = from(g, JRyR, 0), j1 = from(g, JRyR, 1), j2 = from(g, JRyR, 2), j3 = from(g, JRyR, 3);
   const R JRyRtot = j0 + j1 + j2 + j3;
@@ -282,8 +330,9 @@ __device__ __forceinline__ void fcn_fru4(const Group& g, R cajsr, R cass, const 
   const R Jss = divc(cass - cnext, R(tauss2ss), R(1.0 / tauss2ss));
   const R Jss_prev = from(g, Jss, (g.c + 3) & 3);
   const R Jxfer = divc(cass - Cai, R(tauxfer), R(1.0 / tauxfer));
-  const R JDH = small ? R(KJDHsmall) * pca_scale * (cass - R(Cao * 0.341)) * lopen * R(JDHconstant)
-                      : -(cass * e2 - R(Cao * 0.341)) * a2j * lopen;
+  R JDH;
+  if (small) JDH = R(KJDHsmall) * pca_scale * (cass - R(Cao * 0.341)) * lopen * R(JDHconstant);
+  else JDH = -(cass * e2 - R(Cao * 0.341)) * a2j * lopen;
   R a1 = rdiv(R(BSRtot * KBSR), (cass + R(KBSR)) * (cass + R(KBSR)));
   R a2 = rdiv(R(BSLtot * KBSL), (cass + R(KBSL)) * (cass + R(KBSL)));
   const R bSS = rdiv(R(1), R(1) + a1 + a2);
@@ -301,11 +350,18 @@ __device__ __forceinline__ void ghk_terms(R V, R pca_scale, R& e2, R& a2j, bool&
   const R VFRT = divc(V, R(RT_over_F), R(1.0 / RT_over_F));
   const R VFsqRT = R(1000.0 * Faraday) * VFRT;
   e2 = rexp(R(2) * VFRT);
-  small = fabs(V) < R(1.e-6);
-  a2j = small ? R(0) : rdiv(R(PCa * 4.0) * pca_scale * VFsqRT, e2 - R(1)) * R(JDHconstant);
+  small = abs_lt(V, R(1.e-6));
+  if (small) a2j = R(0);
+  else a2j = rdiv(R(PCa * 4.0) * pca_scale * VFsqRT, e2 - R(1)) * R(JDHconstant);
 }
 
-__device__ __forceinline__ double frac_of(double t, double t0, double interval, double) { return (t - t0) / interval; }
+// (t - t0) / interval with r = 1/interval rounded once per stage: Markstein's
+// correction of q = x*r returns the correctly rounded quotient
+__device__ __forceinline__ double frac_of(double t, double t0, double interval, double r) {
+  const double x = t - t0;
+  const double q = x * r;
+  return fma(fma(-q, interval, x), r, q);
+}
 __device__ __forceinline__ float frac_of(double t, double t0, double, float rinterval) {
   return (float)(t - t0) * rinterval;
 }
@@ -355,7 +411,7 @@ __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live
     }
     if (!__any_sync(0xffffffffu, go)) break;
     R cajsr = R(0), cass = R(0), alpha = R(0), beta = R(0), bp = R(0), gam = R(0);
-    R k12 = R(0), k23 = R(0), k34 = R(0), k54 = R(0), k25 = R(0), k56 = R(0);
+    R k12 = R(0), k23 = R(0), k34 = R(0), k54 = R(0), k25 = R(0), k56 = R(0), p34 = R(0);
     R R0[8];
     int regime = 0, ne = 0, pre = 0, etot = 0;
     uint32_t exw[kRyR] = {0u, 0u, 0u, 0u, 0u}, bw[8];
@@ -425,20 +481,38 @@ __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live
     if (go) {
       fetch_new(sc, g, mti, pre, ne, etot, exw, bw);
       {
-        int used = 0;
+        // the draws are taken in order from a shifting window (static
+        // register indices); k34/(k34+k43) is formed once, for the draws of
+        // regimes 0/1 or for the merged state 7 of regime 2 (never both)
+        bool has7 = false, has34 = false;
+  #pragma unroll
+        for (int i = 0; i < kRyR; i++) {
+          const int s = ryr_of(w, i);
+          has7 |= (s == 7);
+          has34 |= (s == 3 || s == 4);
+        }
+        if ((regime <= 1 && has7) || (regime == 2 && (has7 || has34))) p34 = k34 / (k34 + R(k43));
   #pragma unroll
         for (int i = 0; i < kRyR; i++) {
           int s = ryr_of(w, i);
           if (regime == 0) {
             if (s == 7 || s == 8) {
-              const double u = (double)exw[used++] / 4294967296.0;
-              if (s == 7) s = (u < (double)(k34 / (k34 + R(k43)))) ? 4 : 3;
-              else s = (u < (double)(k56 / (k56 + R(k65)))) ? 6 : 5;
+              const uint32_t y = exw[0];
+              exw[0] = exw[1];
+              exw[1] = exw[2];
+              exw[2] = exw[3];
+              exw[3] = exw[4];
+              if (s == 7) s = u_below(y, p34) ? 4 : 3;
+              else s = u_below(y, k56 / (k56 + R(k65))) ? 6 : 5;
             }
           } else if (regime == 1) {
             if (s == 7) {
-              const double u = (double)exw[used++] / 4294967296.0;
-              s = (u < (double)(k34 / (k34 + R(k43)))) ? 4 : 3;
+              const uint32_t y = exw[0];
+              exw[0] = exw[1];
+              exw[1] = exw[2];
+              exw[2] = exw[3];
+              exw[3] = exw[4];
+              s = u_below(y, p34) ? 4 : 3;
             }
             if (s == 5 || s == 6) s = 8;
           } else {
@@ -460,7 +534,7 @@ __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live
         const R T4 = R(k43 + k45);
         R T7 = R(0), T8 = R(0);
         if (need7) {
-          const R a1 = k34 / (R(k43) + k34);
+          const R a1 = p34;  // k34 / (k43 + k34)
           T7 = (R(1) - a1) * R(k32) + a1 * R(k45);
         }
         if (need8) {
@@ -489,7 +563,7 @@ __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live
       // ---- substep size (simfru_local.c:135-146) ----
       R dtr = imin(rdiv(R(0.1), mx), R(10.001e-3));
       const R cmax = gmax(g, imax(R(0.e-3), cass));
-      if (cmax > R(1.5e-3)) dtr = imin(dtr, R(5.001e-3));
+      if (ilt(R(1.5e-3), cmax)) dtr = imin(dtr, R(5.001e-3));
       const double dt64 = imin((double)dtr, p.tf - t);
       const R dt = (R)dt64;
       // ---- Heun step (simfru_local.c:149-173) ----
@@ -508,28 +582,21 @@ __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live
       // ---- transitions of this cleft's 8 channels (:215-276) ----
       bool moved = false;
       if (leave_gt(bw[0], dt, R0[0])) {
-        const LccBasis lb{(double)alpha, (double)beta, (double)bp};
-        double r[4];
+        const LccBasisT<R> lb{alpha, beta, bp};
+        R r[4];
         int d[4];
-        const int len = lcc_row(lcc_of(w), lb, (double)gam, r, d);
-        w = set_field(w, 0, pick_dest(r, d, len, (double)dt, (double)bw[0] / 4294967296.0));
+        const int len = lcc_row(lcc_of(w), lb, gam, r, d);
+        w = set_field(w, 0, choose_dest(r, d, len, dt, bw[0]));
       }
       if (leave_ge(bw[1], dt, R0[1])) w = set_field(w, 4, 3 - vdi_of(w));
   #pragma unroll
       for (int i = 0; i < kRyR; i++) {
         if (leave_gt(bw[2 + i], dt, R0[2 + i])) {
-          RyrK k;
-          k.k12 = k12;
-          k.k23 = k23;
-          k.k34 = k34;
-          k.k54 = k54;
-          k.k25 = k25;
-          k.k56 = k56;
-          k.regime = regime;
-          double r[4];
+          const RyrKT<R> k{k12, k23, k34, k54, k25, k56, regime};
+          R r[4];
           int d[4];
           const int len = ryr_row(ryr_of(w, i), k, r, d);
-          w = set_field(w, 8 + 4 * i, pick_dest(r, d, len, (double)dt, (double)bw[2 + i] / 4294967296.0));
+          w = set_field(w, 8 + 4 * i, choose_dest(r, d, len, dt, bw[2 + i]));
           moved = true;
         }
       }

@@ -136,7 +136,11 @@ struct MtRef {
 };
 
 // ---- LCC: total exit rate and exit row (fru_rates_local.c:131-341) ----------
-struct LccBasis { double alpha, beta, bp; };
+// Rows are templates on the arithmetic type: double for the plain method,
+// float for the mixed-precision one (same expressions, rounded in T).
+template <typename T>
+struct LccBasisT { T alpha, beta, bp; };
+using LccBasis = LccBasisT<double>;
 
 __device__ __forceinline__ LccBasis lcc_basis(double V) {
   LccBasis b;
@@ -148,30 +152,31 @@ __device__ __forceinline__ LccBasis lcc_basis(double V) {
 
 // Exit row of state s: r[0] = total in the reference's summation order,
 // r[1..len-1] with destinations d[1..len-1].
-__device__ __forceinline__ int lcc_row(int s, const LccBasis& b, double gam, double r[4], int d[4]) {
-  const double ap = aL * b.alpha;
+template <typename T>
+__device__ __forceinline__ int lcc_row(int s, const LccBasisT<T>& b, T gam, T r[4], int d[4]) {
+  const T ap = T(aL) * b.alpha;
   switch (s) {
-    case 1: r[1] = 4.0 * b.alpha; d[1] = 2; r[2] = gam; d[2] = 7; r[0] = r[1] + r[2]; return 3;
-    case 2: r[1] = b.beta; d[1] = 1; r[2] = 3.0 * b.alpha; d[2] = 3; r[3] = aL * gam; d[3] = 8;
+    case 1: r[1] = T(4.0) * b.alpha; d[1] = 2; r[2] = gam; d[2] = 7; r[0] = r[1] + r[2]; return 3;
+    case 2: r[1] = b.beta; d[1] = 1; r[2] = T(3.0) * b.alpha; d[2] = 3; r[3] = T(aL) * gam; d[3] = 8;
       r[0] = r[1] + r[2] + r[3]; return 4;
-    case 3: r[1] = 2.0 * b.beta; d[1] = 2; r[2] = 2.0 * b.alpha; d[2] = 4; r[3] = (aL * aL) * gam; d[3] = 9;
+    case 3: r[1] = T(2.0) * b.beta; d[1] = 2; r[2] = T(2.0) * b.alpha; d[2] = 4; r[3] = T(aL * aL) * gam; d[3] = 9;
       r[0] = r[1] + r[2] + r[3]; return 4;
-    case 4: r[1] = 3.0 * b.beta; d[1] = 3; r[2] = b.alpha; d[2] = 5; r[3] = (aL * aL * aL) * gam; d[3] = 10;
+    case 4: r[1] = T(3.0) * b.beta; d[1] = 3; r[2] = b.alpha; d[2] = 5; r[3] = T(aL * aL * aL) * gam; d[3] = 10;
       r[0] = r[1] + r[2] + r[3]; return 4;
-    case 5: r[1] = 4.0 * b.beta; d[1] = 4; r[2] = fL; d[2] = 6; r[3] = (aL * aL * aL * aL) * gam; d[3] = 11;
+    case 5: r[1] = T(4.0) * b.beta; d[1] = 4; r[2] = T(fL); d[2] = 6; r[3] = T(aL * aL * aL * aL) * gam; d[3] = 11;
       r[0] = r[1] + r[2] + r[3]; return 4;
-    case 6: r[0] = gL; r[1] = gL; d[1] = 5; return 2;
-    case 7: r[1] = CCa0_to_C0; d[1] = 1; r[2] = 4.0 * ap; d[2] = 8; r[0] = r[2] + r[1]; return 3;
-    case 8: r[1] = b.bp; d[1] = 7; r[2] = CCa1_to_C1; d[2] = 2; r[3] = 3.0 * ap; d[3] = 9;
+    case 6: r[0] = T(gL); r[1] = T(gL); d[1] = 5; return 2;
+    case 7: r[1] = T(CCa0_to_C0); d[1] = 1; r[2] = T(4.0) * ap; d[2] = 8; r[0] = r[2] + r[1]; return 3;
+    case 8: r[1] = b.bp; d[1] = 7; r[2] = T(CCa1_to_C1); d[2] = 2; r[3] = T(3.0) * ap; d[3] = 9;
       r[0] = r[1] + r[3] + r[2]; return 4;
-    case 9: r[1] = 2.0 * b.bp; d[1] = 8; r[2] = CCa2_to_C2; d[2] = 3; r[3] = 2.0 * ap; d[3] = 10;
+    case 9: r[1] = T(2.0) * b.bp; d[1] = 8; r[2] = T(CCa2_to_C2); d[2] = 3; r[3] = T(2.0) * ap; d[3] = 10;
       r[0] = r[1] + r[3] + r[2]; return 4;
-    case 10: r[1] = 3.0 * b.bp; d[1] = 9; r[2] = CCa3_to_C3; d[2] = 4; r[3] = ap; d[3] = 11;
+    case 10: r[1] = T(3.0) * b.bp; d[1] = 9; r[2] = T(CCa3_to_C3); d[2] = 4; r[3] = ap; d[3] = 11;
       r[0] = r[1] + r[3] + r[2]; return 4;
-    case 11: r[1] = 4.0 * b.bp; d[1] = 10; r[2] = CCa4_to_C4; d[2] = 5; r[3] = fLprime; d[3] = 12;
+    case 11: r[1] = T(4.0) * b.bp; d[1] = 10; r[2] = T(CCa4_to_C4); d[2] = 5; r[3] = T(fLprime); d[3] = 12;
       r[0] = r[1] + r[2] + r[3]; return 4;
-    case 12: r[0] = gLprime; r[1] = gLprime; d[1] = 11; return 2;
-    default: r[0] = 0.0; return 1;
+    case 12: r[0] = T(gLprime); r[1] = T(gLprime); d[1] = 11; return 2;
+    default: r[0] = T(0); return 1;
   }
 }
 
@@ -183,7 +188,9 @@ __device__ __forceinline__ double lcc_total(int s, const LccBasis& b, double gam
 }
 
 // ---- RyR: per-cleft constants and rows (fru_rates_local.c:374-736) ----------
-struct RyrK { double k12, k23, k34, k54, k25, k56; int regime; };
+template <typename T>
+struct RyrKT { T k12, k23, k34, k54, k25, k56; int regime; };
+using RyrK = RyrKT<double>;
 
 __device__ __forceinline__ RyrK ryr_constants(double cass) {
   RyrK k;
@@ -217,26 +224,27 @@ __device__ __forceinline__ int ryr_resolve(int s, const RyrK& k, MtRef& rng) {
 }
 
 // Exit row of a resolved RyR state.
-__device__ __forceinline__ int ryr_row(int s, const RyrK& k, double r[4], int d[4]) {
+template <typename T>
+__device__ __forceinline__ int ryr_row(int s, const RyrKT<T>& k, T r[4], int d[4]) {
   const int g = k.regime;
   switch (s) {
     case 1: r[0] = k.k12; r[1] = k.k12; d[1] = 2; return 2;
-    case 2: r[1] = k21; d[1] = 1; r[2] = k.k23; d[2] = (g == 2) ? 7 : 3; r[3] = k.k25; d[3] = (g == 0) ? 5 : 8;
-      r[0] = k21 + k.k23 + k.k25; return 4;
-    case 3: r[1] = k32; d[1] = 2; r[2] = k.k34; d[2] = 4; r[0] = k32 + k.k34; return 3;
-    case 4: r[1] = k43; d[1] = 3; r[2] = k45; d[2] = (g == 0) ? 5 : 8; r[0] = k43 + k45; return 3;
-    case 5: r[1] = k52; d[1] = 2; r[2] = k.k54; d[2] = 4; r[3] = k.k56; d[3] = 6;
-      r[0] = k52 + k.k54 + k.k56; return 4;
-    case 6: r[0] = k65; r[1] = k65; d[1] = 5; return 2;
+    case 2: r[1] = T(k21); d[1] = 1; r[2] = k.k23; d[2] = (g == 2) ? 7 : 3; r[3] = k.k25; d[3] = (g == 0) ? 5 : 8;
+      r[0] = T(k21) + k.k23 + k.k25; return 4;
+    case 3: r[1] = T(k32); d[1] = 2; r[2] = k.k34; d[2] = 4; r[0] = T(k32) + k.k34; return 3;
+    case 4: r[1] = T(k43); d[1] = 3; r[2] = T(k45); d[2] = (g == 0) ? 5 : 8; r[0] = T(k43) + T(k45); return 3;
+    case 5: r[1] = T(k52); d[1] = 2; r[2] = k.k54; d[2] = 4; r[3] = k.k56; d[3] = 6;
+      r[0] = T(k52) + k.k54 + k.k56; return 4;
+    case 6: r[0] = T(k65); r[1] = T(k65); d[1] = 5; return 2;
     case 7: {
-      const double a1 = k.k34 / (k43 + k.k34);
-      r[1] = (1.0 - a1) * k32; d[1] = 2; r[2] = a1 * k45; d[2] = 8; r[0] = r[1] + r[2]; return 3;
+      const T a1 = k.k34 / (T(k43) + k.k34);
+      r[1] = (T(1) - a1) * T(k32); d[1] = 2; r[2] = a1 * T(k45); d[2] = 8; r[0] = r[1] + r[2]; return 3;
     }
     case 8: {
-      const double a1 = k65 / (k.k56 + k65);
-      r[1] = a1 * k52; d[1] = 2; r[2] = a1 * k.k54; d[2] = (g == 2) ? 7 : 4; r[0] = r[1] + r[2]; return 3;
+      const T a1 = T(k65) / (k.k56 + T(k65));
+      r[1] = a1 * T(k52); d[1] = 2; r[2] = a1 * k.k54; d[2] = (g == 2) ? 7 : 4; r[0] = r[1] + r[2]; return 3;
     }
-    default: r[0] = 0.0; return 1;
+    default: r[0] = T(0); return 1;
   }
 }
 

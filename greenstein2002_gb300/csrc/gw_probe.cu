@@ -48,16 +48,24 @@ cudaError_t probe_fp64(int sms, double* tflops) {
 }
 
 // Cost of the global right-hand side (fcn.c:29-1072) on one GPU thread:
-// `calls` dependent evaluations at the rest state (each call's dV feeds the
-// next call's V by a negligible amount, so none can be skipped).
+// `calls` dependent evaluations at the rest state.  Every derivative and
+// current feeds the next call's V by a negligible amount, so no part of the
+// evaluation can be skipped.
+__host__ __device__ inline double fcn_feedback(const double* F, const double* cur) {
+  double s = 0.0;
+  for (int i = 0; i < GW_NSTATE; i++) s += F[i];
+  for (int i = 0; i < GW_NCUR; i++) s += cur[i];
+  return 1e-300 * s;
+}
+
 __global__ void fcn_chain(const gw_protocol* P, int calls, double* out) {
   double y[GW_NSTATE], F[GW_NSTATE], cur[GW_NCUR];
   gw_rest_state(y);
   for (int i = 0; i < calls; i++) {
     gw_fcn(10.5, y, F, cur, 1, 1e-6, 1e-6, -1e-3, 0.0, P);
-    y[GW_V] = y[GW_V] + 1e-30 * F[GW_V];
+    y[GW_V] = y[GW_V] + fcn_feedback(F, cur);
   }
-  out[0] = y[GW_V] + cur[GW_I_ICa];
+  out[0] = y[GW_V];
 }
 
 cudaError_t probe_fcn(double* device_us, double* host_us) {
@@ -93,10 +101,12 @@ cudaError_t probe_fcn(double* device_us, double* host_us) {
   const auto t0 = std::chrono::steady_clock::now();
   for (int i = 0; i < 20 * calls; i++) {
     gw_fcn(10.5, y, F, cur, 1, 1e-6, 1e-6, -1e-3, 0.0, &hp);
-    y[GW_V] = y[GW_V] + 1e-30 * F[GW_V];
+    y[GW_V] = y[GW_V] + fcn_feedback(F, cur);
   }
   const double us = std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
-  *host_us = us / (20 * calls) + 0.0 * (y[GW_V] + cur[GW_I_ICa]);
+  volatile double sink = y[GW_V];
+  (void)sink;
+  *host_us = us / (20 * calls);
   return e;
 }
 
