@@ -101,6 +101,7 @@ def bind(path):
         "gw_set_fru_lanes": ([vp, C.c_int], C.c_int),
         "gw_set_stage_warps": ([vp, C.c_int], C.c_int),
         "gw_stage_trace": ([vp, C.c_int], C.c_int),
+        "gw_group_timer": ([C.c_int, vp, C.c_int, P(C.c_float)], C.c_int),
         "gw_stage_trace_read": ([vp, vp, vp], C.c_int),
         "gw_batch_set_warps": ([vp, C.c_int], C.c_int),
         "gw_autotune": ([C.c_int, vp, vp, _dp, _dp, _dp, C.c_double, vp, P(C.c_int), P(C.c_int), _dp], C.c_int),
@@ -122,6 +123,7 @@ def bind(path):
         "gw_cell_bytes": ([C.c_int], C.c_size_t),
         "gw_server_create": ([P(vp), C.c_int, C.c_int, C.c_size_t, C.c_int], C.c_int),
         "gw_run_concurrent": ([C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp], C.c_int),
+        "gw_run_device": ([C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp], C.c_int),
         "gw_server_submit": ([vp, P(Request)], C.c_int),
         "gw_server_wait": ([vp], C.c_int),
         "gw_server_destroy": ([vp], C.c_int),
@@ -418,6 +420,45 @@ class Server:
 
 def cell_bytes(nfru):
     return int(load().gw_cell_bytes(int(nfru)))
+
+
+class GroupTimer:
+    """Device time of work the cells run concurrently on their own streams."""
+
+    def __init__(self, cells):
+        self._cells = cells
+        self._L = cells[0]._L
+        self._h = (C.c_void_p * len(cells))(*[c._h.value for c in cells])
+
+    def start(self):
+        _check(self._L.gw_group_timer(len(self._cells), C.cast(self._h, C.c_void_p), 0, None), "gw_group_timer",
+               self._L)
+
+    def stop(self):
+        ms = C.c_float(0.0)
+        _check(self._L.gw_group_timer(len(self._cells), C.cast(self._h, C.c_void_p), 1, C.byref(ms)),
+               "gw_group_timer", self._L)
+        return ms.value
+
+
+def run_device(cells, sets, t, states, oldsteps, n_steps, traces=False, lib=None):
+    """Advance the cells n_steps output steps with the device-resident
+    integrator (gw_run_device); t, states (n, 37) and oldsteps advance in
+    place.  With traces=True returns (states (n, n_steps, 37), otherstates
+    (n, n_steps, 12), currents (n, n_steps, 24))."""
+    L = lib if lib is not None else cells[0]._L
+    n = len(cells)
+    for a in (t, states, oldsteps):
+        assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    handles = (C.c_void_p * n)(*[c._h.value for c in cells])
+    setarr = (Settings * n)(*sets)
+    st_tr = np.zeros((n, n_steps, NSTATE)) if traces else None
+    ot_tr = np.zeros((n, n_steps, NOTHER)) if traces else None
+    cu_tr = np.zeros((n, n_steps, NCUR)) if traces else None
+    _check(L.gw_run_device(n, C.cast(handles, C.c_void_p), C.cast(setarr, C.c_void_p), t.ctypes.data_as(C.c_void_p),
+                           states.ctypes.data_as(C.c_void_p), oldsteps.ctypes.data_as(C.c_void_p), int(n_steps),
+                           _ptr(st_tr), _ptr(ot_tr), _ptr(cu_tr)), "gw_run_device", L)
+    return (st_tr, ot_tr, cu_tr) if traces else None
 
 
 TUNE_CANDIDATES = ((4, 1), (4, 2), (4, 4), (4, 8), (1, 1))

@@ -31,6 +31,7 @@ CUDA_UNITS = {
     "gw_probe.cu": [],
     "gw_noalloc.cu": ["-fmad=false"],
     "gw_tune.cu": [],
+    "gw_devdp.cu": ["-fmad=false"],
 }
 C_UNITS = ["gw_dp.c", "gw_dropin.c"]
 

@@ -409,6 +409,37 @@ extern "C" int gw_substeps(gw_ctx* c, unsigned long long* count) {
   return GW_OK;
 }
 
+// Device time of work that several cells run concurrently on their own
+// streams: phase 0 records a start event on a timing stream and makes every
+// cell's stream wait for it; phase 1 makes the timing stream wait for every
+// cell's stream, records the end event and returns the elapsed ms.
+extern "C" int gw_group_timer(int n, gw_ctx** cells, int phase, float* ms) {
+  static cudaStream_t ts = nullptr;
+  static cudaEvent_t ev[2] = {nullptr, nullptr};
+  static cudaEvent_t link = nullptr;
+  if (n <= 0 || !cells || (phase != 0 && phase != 1) || (phase == 1 && !ms))
+    return set_err(GW_EINVAL, "gw_group_timer: bad argument");
+  if (!ts) {
+    CK(cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&ev[0]));
+    CK(cudaEventCreate(&ev[1]));
+    CK(cudaEventCreateWithFlags(&link, cudaEventDisableTiming));
+  }
+  if (phase == 0) {
+    CK(cudaEventRecord(ev[0], ts));
+    for (int i = 0; i < n; i++) CK(cudaStreamWaitEvent(cells[i]->stream, ev[0], 0));
+    return GW_OK;
+  }
+  for (int i = 0; i < n; i++) {
+    CK(cudaEventRecord(link, cells[i]->stream));
+    CK(cudaStreamWaitEvent(ts, link, 0));
+  }
+  CK(cudaEventRecord(ev[1], ts));
+  CK(cudaEventSynchronize(ev[1]));
+  CK(cudaEventElapsedTime(ms, ev[0], ev[1]));
+  return GW_OK;
+}
+
 extern "C" int gw_stage_trace(gw_ctx* c, int enable) {
   if (!c) return set_err(GW_EINVAL, "gw_stage_trace: null context");
   if (c->batch) return set_err(GW_EINVAL, "gw_stage_trace: change it before the cell joins a batch");

@@ -661,8 +661,47 @@ __device__ __forceinline__ unsigned long long global_ns() {
   return t;
 }
 
-template <typename R>
-__device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, int bidx, double* out) {
+// Where a launch's cell totals go: OutFin writes them to the cell's out[]
+// slots (the host reads them back); the device-resident integrator passes
+// its own finisher.  Called by one lane, with the 5 flux numerators, the
+// currents (Jxfer, Jtr, ICa, Ito2) and, when the launch carried
+// kFlagAvg, the 11 output-average sums (else null).
+struct OutFin {
+  double* out;
+  __device__ void operator()(const double tot[5], const double cur[4], const double*) const {
+#pragma unroll
+    for (int k = 0; k < 5; k++) out[k] = tot[k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[5 + k] = cur[k];
+  }
+  __device__ void error() const { out[kOutError] = 1.0; }
+};
+
+// The 11 output-average terms of one cleft (calc_fru_avg_local.c:27-105):
+// the FRU-level ones (CaJSR and its buffered total) on the cleft-0 lane.
+__device__ __forceinline__ void avg_terms(int c, double jsr, double ss, uint32_t w, double a[11]) {
+  int no = 0, ready = 0;
+#pragma unroll
+  for (int i = 0; i < kRyR; i++) {
+    const int r = ryr_of(w, i);
+    no += ryr_open(r);
+    ready += (r == 1 || r == 2);
+  }
+  a[0] = ss;
+  a[1] = (c == 0) ? jsr : 0.0;
+  a[2] = JRyRmax * ((double)no) * (jsr - ss);
+  a[3] = (double)no;
+  a[4] = (double)ready;
+  a[5] = ss * (1.0 + BSRtot / (KBSR + ss) + BSLtot / (KBSL + ss));
+  a[6] = (c == 0) ? jsr * (1.0 + CSQNtot / (KmCSQN + jsr)) : 0.0;
+  a[7] = (lcc_of(w) <= 6) ? 1.0 : 0.0;
+  a[8] = (vdi_of(w) == 2) ? 1.0 : 0.0;
+  a[9] = lcc_open(w) ? 1.0 : 0.0;
+  a[10] = (cl_of(w) == 2) ? 1.0 : 0.0;
+}
+
+template <typename R, typename Fin>
+__device__ __forceinline__ void stage_body_fin(const DevState& s, const StageParams& p, int bidx, const Fin& fin) {
   extern __shared__ __align__(16) uint32_t mt_stage[];  // [warps][8][kMtSmemStride]
   const int lane = threadIdx.x & 31;
   const int grp = bidx * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
@@ -744,11 +783,30 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, in
   }
   __syncwarp();
   if (s.trace_ns && lane == 0) s.trace_ns[2 * grp + 1] = global_ns();
-  if (overflow) out[kOutError] = 1.0;
+  if (overflow) fin.error();
   if (s.substeps) {
     unsigned long long c = (g.c == 0) ? nsub : 0;
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
     if (lane == 0 && c) atomicAdd(s.substeps, c);
+  }
+  if (p.flags & kFlagAvg) {
+    // flux numerators and output averages in one pass (16 partials per group)
+    double u[16];
+#pragma unroll
+    for (int k = 0; k < 5; k++) u[k] = v[k];
+    double a[11];
+    avg_terms(g.c, cajsr, cass, w, a);
+#pragma unroll
+    for (int k = 0; k < 11; k++) u[5 + k] = active ? a[k] : 0.0;
+    warp_sum<16>(u);
+    double tot[16];
+    if (cell_finish<16>(u, s.partials, s.ticket, tot, grp, ngroups)) {
+      double cur[4];
+      currents_from_sums(s.nfru, p.nfru_scale, p.depf, tot, cur);
+      cur[2] = cur[2] * p.pca_scale;  // ICa is proportional to the LCC permeability
+      fin(tot, cur, tot + 5);
+    }
+    return;
   }
   warp_sum<5>(v);
   double tot[5];
@@ -756,11 +814,13 @@ __device__ __forceinline__ void stage_body(DevState& s, const StageParams& p, in
     double cur[4];
     currents_from_sums(s.nfru, p.nfru_scale, p.depf, tot, cur);
     cur[2] = cur[2] * p.pca_scale;  // ICa is proportional to the LCC permeability
-#pragma unroll
-    for (int k2 = 0; k2 < 5; k2++) out[k2] = tot[k2];
-#pragma unroll
-    for (int k2 = 0; k2 < 4; k2++) out[5 + k2] = cur[k2];
+    fin(tot, cur, nullptr);
   }
+}
+
+template <typename R>
+__device__ __forceinline__ void stage_body(const DevState& s, const StageParams& p, int bidx, double* out) {
+  stage_body_fin<R>(s, p, bidx, OutFin{out});
 }
 
 // ---- many cells in one launch ------------------------------------------------
@@ -776,8 +836,10 @@ __device__ __forceinline__ void batch_body(const BatchArgs& a) {
     if (__ldg(&a.block0[mid]) <= b) lo = mid;
     else hi = mid - 1;
   }
-  DevState s = a.cells[lo];
-  const StageParams p = a.params[lo];
+  // the cell's arrays and parameters are read where used (through L1)
+  // rather than copied into registers
+  const DevState& s = a.cells[lo];
+  const StageParams& p = a.params[lo];
   if (p.flags < 0) return;  // the cell posted no operation this round
   stage_body<R>(s, p, b - a.block0[lo], a.outs + kBatchOutStride * lo);
 }

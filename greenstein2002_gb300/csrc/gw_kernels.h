@@ -36,6 +36,7 @@ enum : int {
   kFlagAdvance = 1,  // run the substep loop over [t0, tf]
   kFlagSave = 2,     // snapshot FRU state before advancing (send_save_state)
   kFlagResume = 4,   // restore the snapshot before advancing (send_resume_state)
+  kFlagAvg = 8,      // also reduce the 11 output-average sums (calc_fru_avg_local)
 };
 enum : int { kSeedBase = 0, kSeedReference = 1 };
 

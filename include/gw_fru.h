@@ -113,6 +113,10 @@ int gw_sync(gw_ctx *ctx);
 int gw_event_record(gw_ctx *ctx, int slot);
 int gw_event_elapsed(gw_ctx *ctx, int slot_a, int slot_b, float *ms);
 int gw_profile(gw_ctx *ctx, int enable);
+/* Device time of work several cells run concurrently on their own streams
+ * (no reference counterpart): phase 0 before the work, phase 1 after it
+ * returns the elapsed ms in *ms.  Not thread-safe; one group at a time. */
+int gw_group_timer(int n, gw_ctx **cells, int phase, float *ms);
 /* Stage trace (diagnostics of the 4-lane kernels; no reference
  * counterpart): when enabled, every stage launch records each FRU's substep
  * count and each 8-FRU warp's begin and end global time in ns;
@@ -217,6 +221,17 @@ int gw_batch_run(gw_batch *batch, int n, gw_ctx **cells, const gw_settings *sets
  * thread, its kernels running concurrently with the others'. */
 int gw_run_concurrent(int n, gw_ctx **cells, const gw_settings *sets, double *t, double *states, double *oldsteps,
                       int n_steps, double *state_trace, double *other_trace);
+/* Device-resident integrator (the level-B seam of rk54pd, rk_pd54m.c:29):
+ * n cells advance n_steps output steps each with their Dormand-Prince
+ * integrators on the GPU -- one CUDA graph whose WHILE loop runs rounds of
+ * [every cell's FRU launch, every cell's integrator step] until all cells
+ * are done; no host round trip inside a step.  Arguments as gw_batch_run,
+ * plus cur_trace [n][n_steps][24] (may be NULL).  Cells must share one
+ * precision and not be in a batch.  Same arithmetic as gw_run, except that
+ * the global right-hand side uses CUDA's exp/pow/log (last-place
+ * differences from the host C library). */
+int gw_run_device(int n, gw_ctx **cells, const gw_settings *sets, double *t, double *states, double *oldsteps,
+                  int n_steps, double *state_trace, double *other_trace, double *cur_trace);
 /* Warps per block of the batch's launches (1, 2, 4 or 8; same results). */
 int gw_batch_set_warps(gw_batch *batch, int warps);
 
