@@ -1,28 +1,34 @@
-"""Benchmark: cell-ms simulated per second for one 12,500-FRU cell.
+"""Benchmark: cell-ms simulated per second at 12,500 FRUs per cell.
 
-Workload (the full-size plain FP64 configuration): one cell of NFRU=12,500
-release units, rest initial state (initialize_state.c:164-219), per-FRU
-MT19937 seeded 5489+j, 1 Hz pacing with a 1 ms -100 uA/uF stimulus at
-10 ms.  A step advances the cell by STEP_MS (10 ms) of simulated time through
-the whole hot path (Dormand-Prince global step, every FRU stage on the GPU).
-Warm-up steps cover [0, W*10) ms (the stimulus and upstroke), so with the
-defaults (W=3, K=20) the timed window is [30, 230) ms: the plateau of the
-first beat, when Ca release keeps the most FRUs busy -- more FRU-substeps per
-ms than the beat average, so the rate is a conservative one.  L2 (129 MB) is
-flushed by a 512 MB write between timed steps.
+Workload (the full-size plain FP64 configuration: one cell of NFRU=12,500
+release units per seed, rest initial state (initialize_state.c:164-219), 1 Hz
+pacing with a 1 ms -100 uA/uF stimulus at 10 ms, 64 seeds for ensemble
+statistics): `value` is the throughput of an ensemble of --seeds cells (cell
+k's FRU j seeded 5489 + 100000 k + j) running on the GPU at once, one stream
+and one host integrator thread per cell -- the same kind of throughput the
+reference arm measures with one cell per host core.  Four cells already keep
+the FP64 pipe saturated (1, 4, 16 and 64 cells gave 8.5, 14.4, 14.4 and 14.4
+cell-ms/s over [30, 40) ms).  A step advances every cell by STEP_MS (10 ms) of
+simulated time through the whole hot path (Dormand-Prince global step, every
+FRU stage on the GPU).  Warm-up steps cover [0, W*10) ms (the stimulus and
+upstroke), so with the defaults (W=3, K=20) the timed window is [30, 230) ms:
+the plateau and early repolarisation of the first beat.  L2 (129 MB) is
+flushed by a 512 MB write between timed steps.  Each step is timed on the
+device (events on a timing stream joined to every cell's stream).
 
-Beside the FP64 value the line carries the same window in mixed precision
-("mixed", with its error against the FP64 run), a batched run ("batched":
-64 cells of NFRU 1250-12,500 with varied pacing and conductances running
+Beside it the line carries one cell alone ("one_cell": the latency of the
+plain method, CUDA events on its stream), the same window in mixed precision
+("mixed", with its error against the FP64 run), a batched run ("batched": 64
+cells of NFRU 1250-12,500 with varied pacing and conductances running
 concurrently, mixed precision) and a serving sweep ("serving": Poisson
 arrivals of cell requests, p50/p99 latency).  Before each timed section the
 launch-shape autotuner picks lanes per FRU and warps per block on the
 section's own workload ("tuning"; results do not depend on the choice).
 
-value: inputs resident in HBM, device-timed with CUDA events on the library's
-stream.  e2e: the same window through the C-ABI with host buffers: every
-step uploads the cell's full FRU + RNG state from host memory (gw_upload)
-and downloads it and the step's traces (gw_download) inside the timed region.
+value: inputs resident in HBM.  e2e: the ensemble's window through the C-ABI
+with host buffers: every step uploads each cell's full FRU + RNG state from
+host memory (gw_upload) and downloads it and the step's traces (gw_download)
+inside the timed region.
 
 --impl reference: the reference's own serial program (oracle/_ref, built
 from its sources) on the host cores, one independent 12,500-FRU cell per
@@ -50,6 +56,10 @@ SEED = 5489
 # algorithmic work per FRU-substep (static count of the reference's substep:
 # fru_rates_local + 2 x fcn_fru + simfru_local body, each add/mul/div/exp/
 # compare/convert counted once) and MT19937 bytes streamed per substep
+# DRAM bytes per stage launch of a 12,500-FRU cell: ncu's dram__bytes_read +
+# dram__bytes_write of a 2,500-FRU plateau launch (6.67 MB, cold L2 per
+# replay) times 5 (the bytes are per FRU: its state and MT row).
+TRAFFIC_PER_LAUNCH_12500 = 5 * 6.672128e6
 FLOPS_PER_SUBSTEP = 700.0
 BYTES_PER_SUBSTEP = 384.0
 
@@ -61,6 +71,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gw", choices=["gw", "reference"])
     ap.add_argument("--nfru", type=int, default=NFRU)
+    ap.add_argument("--seeds", type=int, default=4,
+                    help="cells of the FP64 ensemble (seeds k: FRU j seeded 5489 + 100000 k + j) run at once")
     ap.add_argument("--step-ms", type=float, default=STEP_MS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -73,6 +85,7 @@ def parse():
     ap.add_argument("--batch-mode", default="streams", choices=["streams", "lockstep"],
                     help="streams: each cell on its own stream; lockstep: shared batched launches")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-devdp", action="store_true", help="skip the device-integrator batched run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--tune-ms", type=float, default=2.0, help="simulated window per autotuner candidate")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[1.0, 10.0, 50.0, 200.0])
@@ -334,6 +347,102 @@ def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
     return out
 
 
+def ensemble(G, args, dist, precision):
+    """args.seeds independent cells of args.nfru FRUs, rest state, 1 Hz pacing;
+    cell k's FRU j is seeded 5489 + 100000 (k + seeds * rank) + j."""
+    import numpy as np
+    cells, sets, states = [], [], []
+    for k in range(args.seeds):
+        c = G.Cell(args.nfru, fru_lanes=args.fru_lanes, precision=precision)
+        st = G.settings()
+        states.append(c.init_rest(st, scheme=G.SEED_BASE, base=SEED + 100000 * (k + args.seeds * dist.rank)))
+        cells.append(c)
+        sets.append(st)
+    return cells, sets, np.ascontiguousarray(np.array(states))
+
+
+def time_ensemble(G, args, dist, precision, clocks=None):
+    """The ensemble on the GPU at once (one stream and host driver thread per
+    cell): W warm-up steps, the launch-shape autotuner, then K timed steps,
+    each timed on the device from before the first cell's first launch to
+    after the last cell's last one (gw_group_timer), L2 flushed between
+    steps."""
+    import numpy as np
+    cells, sets, states = ensemble(G, args, dist, precision)
+    n = len(cells)
+    t = np.zeros(n)
+    old = np.full(n, 0.1)
+    runner = G.Batch(precision)
+    step = int(args.step_ms)
+    for _ in range(args.warmup):
+        runner.run(cells, sets, t, states, old, step, lockstep=False)
+    tuning = None
+    if not args.no_autotune and args.fru_lanes == 4:
+        tuning = tune_summary(G.autotune(cells, sets, t, states, old, args.tune_ms), args)
+    sub0 = sum(c.substeps() for c in cells)
+    launch0 = sum(c.launches() for c in cells)
+    timer = G.GroupTimer(cells)
+    total_ms = 0.0
+    dist.barrier()
+    for c in cells:
+        c.sync()
+    if clocks:
+        clocks.start()
+    for _ in range(args.steps):
+        cells[0].l2_flush()
+        timer.start()
+        runner.run(cells, sets, t, states, old, step, lockstep=False)
+        total_ms += timer.stop()
+    clk = clocks.stop() if clocks else None
+    dist.barrier()
+    out = {"device_ms": dist.max(total_ms), "substeps": sum(c.substeps() for c in cells) - sub0,
+           "launches": sum(c.launches() for c in cells) - launch0, "clocks": clk, "tuning": tuning, "cells": n}
+    out["value"] = dist.sum(n * args.steps * args.step_ms) / (out["device_ms"] / 1000.0)
+    for c in cells:
+        c.close()
+    runner.close()
+    return out
+
+
+def time_ensemble_e2e(G, args, dist, precision, tuning=None):
+    """The ensemble's timed window through the C-ABI with host buffers: every
+    step uploads each cell's full FRU + RNG state and global state from host
+    memory, runs the step, and downloads them and the step's traces."""
+    import numpy as np
+    cells, sets, states = ensemble(G, args, dist, precision)
+    n = len(cells)
+    if tuning:
+        for c in cells:
+            c.set_fru_lanes(tuning["lanes_per_fru"])
+            c.set_stage_warps(tuning["warps_per_block"])
+    t = np.zeros(n)
+    old = np.full(n, 0.1)
+    runner = G.Batch(precision)
+    step = int(args.step_ms)
+    for _ in range(args.warmup):
+        runner.run(cells, sets, t, states, old, step, lockstep=False)
+    host = [c.download() for c in cells]
+    h_states = states.copy()
+    h2d = sum(v.nbytes for h in host for v in h.values()) + h_states.nbytes
+    dist.barrier()
+    e2e_s, d2h = 0.0, 0
+    for _ in range(args.steps):
+        cells[0].l2_flush()
+        t0 = time.perf_counter()
+        for c, h in zip(cells, host):
+            c.upload(h)
+        st_tr, ot_tr = runner.run(cells, sets, t, h_states, old, step, traces=True, lockstep=False)
+        host = [c.download() for c in cells]
+        e2e_s += time.perf_counter() - t0
+        d2h = sum(v.nbytes for h in host for v in h.values()) + st_tr.nbytes + ot_tr.nbytes
+    dist.barrier()
+    for c in cells:
+        c.close()
+    runner.close()
+    return {"value": dist.sum(n * args.steps * args.step_ms) / dist.max(e2e_s), "unit": "cell-ms/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+
 def time_e2e(G, args, dist, seed, tuning=None):
     """The same window through the C-ABI with host buffers: the cell's full FRU +
     RNG state is uploaded and downloaded, and its traces read back, every step."""
@@ -368,10 +477,10 @@ def time_e2e(G, args, dist, seed, tuning=None):
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
 
 
-def time_batched(G, args, dist):
-    """Many cells sharing each stage launch (gw_batch), mixed precision: NFRU drawn
-    from {1250, 2500, 5000, 12500}, pacing cycle length U(300, 2000) ms, PCa and
-    GKr scaled by lognormal(0, 0.2) factors; one host thread per cell."""
+def batch_cells(G, args, dist):
+    """The batched workload, mixed precision: NFRU drawn from {1250, 2500,
+    5000, 12500}, pacing cycle length U(300, 2000) ms, PCa and GKr scaled by
+    lognormal(0, 0.2) factors."""
     import numpy as np
     rng = np.random.default_rng(20021 + dist.rank)
     n = args.batch_cells
@@ -384,7 +493,41 @@ def time_batched(G, args, dist):
         states.append(c.init_rest(st, scheme=G.SEED_BASE, base=SEED + 100003 * i))
         cells.append(c)
         sets.append(st)
-    states = np.ascontiguousarray(np.array(states))
+    return sizes, cells, sets, np.ascontiguousarray(np.array(states))
+
+
+def time_batched_device(G, args, dist):
+    """The batched workload with the device-resident integrator
+    (gw_run_device): all cells' integrators and FRU stages in one CUDA graph,
+    no host thread per cell."""
+    import numpy as np
+    sizes, cells, sets, states = batch_cells(G, args, dist)
+    n = len(cells)
+    t = np.zeros(n)
+    old = np.full(n, 0.1)
+    G.run_device(cells, sets, t, states, old, args.batch_warmup_ms)
+    sub0 = sum(c.substeps() for c in cells)
+    dist.barrier()
+    t0 = time.perf_counter()
+    G.run_device(cells, sets, t, states, old, args.batch_ms)
+    wall = time.perf_counter() - t0
+    substeps = sum(c.substeps() for c in cells) - sub0
+    eq_ms = float(np.sum(sizes)) / NFRU * args.batch_ms
+    for c in cells:
+        c.close()
+    return {"value": dist.sum(n * args.batch_ms) / dist.max(wall), "unit": "cell-ms/s (cells of mixed NFRU)",
+            "value_12500_equiv": dist.sum(eq_ms) / dist.max(wall), "cells": n,
+            "window_ms": [args.batch_warmup_ms, args.batch_warmup_ms + args.batch_ms],
+            "fru_substeps_per_s": substeps / wall, "precision": "mixed",
+            "timing": "host wall clock around one graph launch (the run is one CUDA graph)"}
+
+
+def time_batched(G, args, dist):
+    """Many cells at once (per-stream or lockstep gw_batch), one host
+    integrator thread per cell; the workload of batch_cells."""
+    import numpy as np
+    sizes, cells, sets, states = batch_cells(G, args, dist)
+    n = len(cells)
     t = np.zeros(n)
     old = np.full(n, 0.1)
     b = G.Batch("mixed")
@@ -473,23 +616,30 @@ def run_gpu(args, dist):
     G.load()
     seed = SEED + dist.rank * args.nfru  # replicas: independent streams per rank
     clocks = Clocks(dist.local)
-    main = time_single(G, args, dist, args.precision, seed, keep_trace=True, clocks=clocks)
-    wall_ms, substeps = main["wall_ms"], main["substeps"]
-    # roofline of the dominant kernel (the FRU stage kernel), FP64-pipe bound;
-    # the FP64 peak is measured in this run
+    # headline: the FP64 ensemble, all cells on the GPU at once
+    ens = time_ensemble(G, args, dist, args.precision, clocks=clocks)
+    substeps = ens["substeps"]
+    # roofline of the dominant kernel (the FRU stage kernel, 98-99% of the
+    # device time), FP64-pipe bound: algorithmic FLOPs of all its launches in
+    # the timed region over the region's device time (the cells' launches
+    # overlap); the FP64 peak is measured in this run
     fp64_peak = G.fp64_peak_tflops()
-    per_launch_ms = main["kern_ms"] / max(main["kern_launches"], 1)
-    sub_per_launch = substeps / max(main["kern_launches"], 1)
-    achieved_tf = FLOPS_PER_SUBSTEP * sub_per_launch / (per_launch_ms * 1e-3) / 1e12
-    achieved_gbs = BYTES_PER_SUBSTEP * sub_per_launch / (per_launch_ms * 1e-3) / 1e9
+    achieved_tf = FLOPS_PER_SUBSTEP * substeps / (ens["device_ms"] * 1e-3) / 1e12
+    achieved_gbs = BYTES_PER_SUBSTEP * substeps / (ens["device_ms"] * 1e-3) / 1e9
     hbm_peak = load_peaks().get("hbm_gbs", 6800.0)
+    # one cell alone (the latency of the plain method; the denominator of the
+    # mixed, batched and serving speed-ups)
+    one = time_single(G, args, dist, args.precision, seed, keep_trace=True)
+    one_line = {"value": one["value"], "unit": "cell-ms/s", "fru_substeps_per_s": one["substeps"] / (one["wall_ms"] / 1e3),
+                "per_launch_ms": one["kern_ms"] / max(one["kern_launches"], 1), "launches": int(one["kern_launches"]),
+                "tuning": one["tuning"], "timing": "CUDA events on the cell's stream"}
 
     mixed = None
     if args.precision == "fp64" and not args.no_mixed:
         m = time_single(G, args, dist, "mixed", seed, keep_trace=True)
-        a, b = main["trace"], m["trace"]
+        a, b = one["trace"], m["trace"]
         cai_range = float(np.max(a[:, 6]) - np.min(a[:, 6])) or 1.0
-        mixed = {"value": m["value"], "unit": "cell-ms/s", "speedup_vs_fp64": m["value"] / main["value"],
+        mixed = {"value": m["value"], "unit": "cell-ms/s (one cell)", "speedup_vs_fp64_one_cell": m["value"] / one["value"],
                  "fru_substeps_per_s": m["substeps"] / (m["wall_ms"] / 1000.0), "tuning": m["tuning"],
                  "error_vs_fp64_same_seeds": {
                      "max_abs_dV_mV": float(np.max(np.abs(a[:, 0] - b[:, 0]))),
@@ -497,6 +647,10 @@ def run_gpu(args, dist):
                      "max_rel_dCaNSR": float(np.max(np.abs(a[:, 7] - b[:, 7]) / np.abs(a[:, 7]))),
                      "window": "per-ms global states over the timed window"}}
     batched = None if args.no_batch else time_batched(G, args, dist)
+    if batched:
+        batched["speedup_12500_equiv_vs_fp64_one_cell"] = batched["value_12500_equiv"] / one["value"]
+        if not args.no_devdp:
+            batched["device_integrator"] = time_batched_device(G, args, dist)
     serving = None
     if not args.no_serve and dist.world == 1:
         serving = {"protocol": "per request: %g ms from rest, NFRU in {1250,2500,5000,12500}, 50/50 pacing "
@@ -504,7 +658,9 @@ def run_gpu(args, dist):
                                "%d worker slots, %g GB admission budget" % (args.serve_ms, args.serve_slots,
                                                                             args.serve_budget_gb),
                    "sweep": [time_serving(G, args, r) for r in args.serve_rates]}
-    e2e = None if args.no_e2e else time_e2e(G, args, dist, seed, main["tuning"])
+        for r in serving["sweep"]:
+            r["speedup_12500_equiv_vs_fp64_one_cell"] = r["cell_ms_per_s_12500_equiv"] / one["value"]
+    e2e = None if args.no_e2e else time_ensemble_e2e(G, args, dist, args.precision, ens["tuning"])
 
     # ---- CPU baseline: the reference program on one host core ----
     cpu = None
@@ -524,35 +680,42 @@ def run_gpu(args, dist):
     if dist.rank == 0:
         kernel = ("fru_stage_mixed_kernel" if args.precision == "mixed" else
                   "fru_stage4_kernel" if args.fru_lanes == 4 else "fru_stage_kernel")
+        window = "[%g, %g) ms" % (args.warmup * args.step_ms, (args.warmup + args.steps) * args.step_ms)
         line = {
-            "metric": "cell-ms simulated/s at 12,500 FRUs", "value": main["value"], "unit": "cell-ms/s",
+            "metric": "cell-ms simulated/s at 12,500 FRUs", "value": ens["value"], "unit": "cell-ms/s",
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": wall_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": ens["device_ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
-            "config": {"workload": "one cell per GPU, NFRU=%d, rest state, 1 Hz pacing (1 ms -100 uA/uF at 10 ms), "
-                                   "seeds 5489+j; step = %g ms simulated; timed window [%g, %g) ms"
-                                   % (args.nfru, args.step_ms, args.warmup * args.step_ms,
-                                      (args.warmup + args.steps) * args.step_ms),
-                       "nfru": args.nfru, "step_ms": args.step_ms,
+            "config": {"workload": "FP64 ensemble of %d cells per GPU (%d of the 64 seeds; cell k's FRU j seeded "
+                                   "5489+100000k+j), NFRU=%d each, rest state, 1 Hz pacing (1 ms -100 uA/uF at 10 ms), "
+                                   "all cells on the GPU at once; step = %g ms simulated per cell; timed window %s"
+                                   % (args.seeds, args.seeds, args.nfru, args.step_ms, window),
+                       "nfru": args.nfru, "cells": args.seeds, "step_ms": args.step_ms,
                        "precision": ("fp64 (FRU path and global ODE)" if args.precision == "fp64" else
                                      "mixed (FRU rates and local Ca ODE fp32; FRU state, clock, flux sums "
                                      "and global ODE fp64)"),
-                       "integrator": "host Dormand-Prince 5(4), FRU stages on GPU",
+                       "integrator": "host Dormand-Prince 5(4) per cell, FRU stages on GPU",
                        "fru_lanes": args.fru_lanes,
                        "l2": "flushed between timed steps (512 MB write)",
+                       "timing": "device time of each step from before the first cell's first launch to after the "
+                                 "last cell's last launch (events on a timing stream joined to every cell's stream)",
                        "parallelism": "replicas" if dist.world > 1 else "single GPU"},
-            "fru_substeps": int(substeps), "fru_substeps_per_s": substeps / (wall_ms / 1000.0),
-            "gpu_launches": int(main["launches"]),
+            "fru_substeps": int(substeps), "fru_substeps_per_s": substeps / (ens["device_ms"] / 1000.0),
+            "gpu_launches": int(ens["launches"]),
             "roofline": {"bound": "fp64", "kernel": kernel, "achieved": achieved_tf,
                          "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak if fp64_peak else None,
                          "peak_source": "measured in-run (independent DFMA chains on all SMs)",
-                         "traffic": None, "per_launch_ms": per_launch_ms, "launches": int(main["kern_launches"]),
-                         "algorithmic": "%g FLOP x %.0f FRU-substeps per launch" % (FLOPS_PER_SUBSTEP, sub_per_launch),
+                         "traffic": TRAFFIC_PER_LAUNCH_12500 if args.nfru == NFRU else None,
+                         "traffic_note": "bytes per stage launch of a 12,500-FRU cell, from one ncu capture scaled "
+                                         "from 2,500 FRUs (cold L2 per replay; in the run the cells stay in L2)",
+                         "algorithmic": "%g FLOP per FRU-substep x %d FRU-substeps over the timed region's device time"
+                                        % (FLOPS_PER_SUBSTEP, substeps),
                          "hbm_view": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                                       "frac": achieved_gbs / hbm_peak,
                                       "algorithmic": "%g B x FRU-substeps" % BYTES_PER_SUBSTEP}},
-            "clocks": main["clocks"],
-            "tuning": main["tuning"],
+            "clocks": ens["clocks"],
+            "tuning": ens["tuning"],
+            "one_cell": one_line,
             "mixed": mixed,
             "batched": batched,
             "serving": serving,
