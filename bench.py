@@ -296,11 +296,26 @@ def load_peaks():
         return {}
 
 
+def _shape_name(k):
+    lanes, warps = k
+    return "packed_%d_fru_per_warp" % (8 * -warps) if warps < 0 else "%d_lanes_%d_warps" % (lanes, warps)
+
+
 def tune_summary(res, args):
     lanes, warps, ms = res
-    return {"lanes_per_fru": lanes, "fru_per_warp": 32 // lanes, "warps_per_block": warps,
+    packed = warps < 0
+    return {"lanes_per_fru": lanes, "fru_per_warp": 8 * -warps if packed else 32 // lanes,
+            "warps_per_block": 1 if packed else warps, "packed_div": -warps if packed else 0,
             "window_ms": args.tune_ms,
-            "candidates_ms": {"%d_lanes_%d_warps" % k: round(v, 2) for k, v in sorted(ms.items())}}
+            "candidates_ms": {_shape_name(k): round(v, 2) for k, v in sorted(ms.items())}}
+
+
+def apply_tuning(cell, tuning):
+    """Give another cell the shape the autotuner chose (results never depend on it)."""
+    cell.set_fru_lanes(tuning["lanes_per_fru"])
+    cell.set_stage_warps(tuning["warps_per_block"])
+    div = tuning.get("packed_div", 0)
+    cell.set_stage_packing(((cell.nfru + 7) // 8 + div - 1) // div if div else 0)
 
 
 def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
@@ -413,8 +428,7 @@ def time_ensemble_e2e(G, args, dist, precision, tuning=None):
     n = len(cells)
     if tuning:
         for c in cells:
-            c.set_fru_lanes(tuning["lanes_per_fru"])
-            c.set_stage_warps(tuning["warps_per_block"])
+            apply_tuning(c, tuning)
     t = np.zeros(n)
     old = np.full(n, 0.1)
     runner = G.Batch(precision)
@@ -448,8 +462,7 @@ def time_e2e(G, args, dist, seed, tuning=None):
     RNG state is uploaded and downloaded, and its traces read back, every step."""
     cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, args.precision)
     if tuning:
-        cell.set_fru_lanes(tuning["lanes_per_fru"])
-        cell.set_stage_warps(tuning["warps_per_block"])
+        apply_tuning(cell, tuning)
     t = 0.0
     oldstep = st.step_max
     n = int(args.step_ms)

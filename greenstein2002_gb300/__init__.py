@@ -100,6 +100,7 @@ def bind(path):
         "gw_sync": ([vp], C.c_int),
         "gw_set_fru_lanes": ([vp, C.c_int], C.c_int),
         "gw_set_stage_warps": ([vp, C.c_int], C.c_int),
+        "gw_set_stage_packing": ([vp, C.c_int], C.c_int),
         "gw_stage_trace": ([vp, C.c_int], C.c_int),
         "gw_group_timer": ([C.c_int, vp, C.c_int, P(C.c_float)], C.c_int),
         "gw_stage_trace_read": ([vp, vp, vp], C.c_int),
@@ -199,6 +200,9 @@ class Cell:
         _check(self._L.gw_stage_trace_read(self._h, sub.ctypes.data_as(C.c_void_p), ns.ctypes.data_as(C.c_void_p)),
                "gw_stage_trace_read", self._L)
         return sub, ns
+
+    def set_stage_packing(self, warps):
+        _check(self._L.gw_set_stage_packing(self._h, int(warps)), "gw_set_stage_packing", self._L)
 
     def set_fru_lanes(self, lanes):
         _check(self._L.gw_set_fru_lanes(self._h, int(lanes)), "gw_set_fru_lanes", self._L)
@@ -461,7 +465,9 @@ def run_device(cells, sets, t, states, oldsteps, n_steps, traces=False, lib=None
     return (st_tr, ot_tr, cu_tr) if traces else None
 
 
-TUNE_CANDIDATES = ((4, 1), (4, 2), (4, 4), (4, 8), (1, 1))
+# (lanes per FRU, warps per block), or (4, -2) / (4, -4) / (4, -8): packed
+# launches with a half / a quarter / an eighth as many warps as 8-FRU groups
+TUNE_CANDIDATES = ((4, 1), (4, 2), (4, 4), (4, 8), (1, 1), (4, -2), (4, -4), (4, -8))
 
 
 def autotune(cells, sets, t, states, oldsteps, window_ms, batch=None, lib=None):

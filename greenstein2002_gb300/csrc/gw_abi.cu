@@ -36,7 +36,18 @@ static int set_err(int code, const char* fmt, ...) {
                                           __FILE__, __LINE__);                                  \
   } while (0)
 
-static cudaError_t launch_stage_variant(gw_ctx* c, const StageParams& p) {
+static cudaError_t launch_stage_variant(gw_ctx* c, const StageParams& p0) {
+  StageParams p = p0;
+  p.launch = c->pack_launch;
+  if (c->packed_warps > 0 && c->fru_lanes == 4 && (p.flags & gw::kFlagAdvance)) {
+    // packed: advance from the queue, then the sums over the stored states
+    cudaError_t e = (c->precision == 1) ? gw::launch_stage_mixed_packed(c->d, p, c->packed_warps, c->stream)
+                                        : gw::launch_stage4_packed(c->d, p, c->packed_warps, c->stream);
+    if (e != cudaSuccess) return e;
+    p.flags = gw::kFlagQueueReset;
+    c->pack_launch++;
+    c->launches++;
+  }
   if (c->precision == 1) return gw::launch_stage_mixed(c->d, p, c->stage_warps, c->stream);
   return c->fru_lanes == 4 ? gw::launch_stage4(c->d, p, c->stage_warps, c->stream)
                            : gw::launch_stage(c->d, p, c->stream);
@@ -52,7 +63,7 @@ extern "C" int gw_nfru(const gw_ctx* c) { return c ? c->d.nfru : 0; }
 static void free_dev(gw_ctx* c) {
   void* ptrs[] = {c->d.frus, c->d.chan, c->d.mti, c->d.mt, c->d.frus_s, c->d.chan_s, c->d.mti_s,
                   c->d.mt_hold, c->d.hold_epoch, c->d.partials, c->d.ticket, c->d.out, c->d.substeps,
-                  c->d.trace_sub, c->d.trace_ns};
+                  c->d.trace_sub, c->d.trace_ns, c->d.qctl, c->d.heavy_list, c->d.heavy_tag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -94,6 +105,9 @@ extern "C" int gw_create(gw_ctx** out, int nfru) {
   AL(d.ticket, sizeof(unsigned));
   AL(d.out, 32 * sizeof(double));
   AL(d.substeps, sizeof(unsigned long long));
+  AL(d.qctl, 8 * sizeof(unsigned));
+  AL(d.heavy_list, 2 * nf * sizeof(int));
+  AL(d.heavy_tag, 2 * nf * sizeof(uint32_t));
 #undef AL
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_out, 32 * sizeof(double));
@@ -103,6 +117,8 @@ extern "C" int gw_create(gw_ctx** out, int nfru) {
   if (e == cudaSuccess) e = cudaMemsetAsync(d.out, 0, 32 * sizeof(double), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.substeps, 0, sizeof(unsigned long long), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.hold_epoch, 0xff, nf * sizeof(uint32_t), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.qctl, 0, 8 * sizeof(unsigned), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d.heavy_tag, 0, 2 * nf * sizeof(uint32_t), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.frus, 0, 5 * nf * sizeof(double), c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d.chan, 0, 4 * nf * sizeof(uint32_t), c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -144,6 +160,13 @@ extern "C" int gw_set_stage_warps(gw_ctx* c, int warps) {
   if (!c || warps < 1 || warps > gw::kMaxStageWarps || (warps & (warps - 1)))
     return set_err(GW_EINVAL, "gw_set_stage_warps: warps per block must be 1, 2, 4 or 8");
   c->stage_warps = warps;
+  return GW_OK;
+}
+
+extern "C" int gw_set_stage_packing(gw_ctx* c, int warps) {
+  if (!c || warps < 0) return set_err(GW_EINVAL, "gw_set_stage_packing: warps must be >= 0");
+  const int groups = (c->d.nfru + 7) / 8;
+  c->packed_warps = warps > groups ? groups : warps;
   return GW_OK;
 }
 

@@ -24,6 +24,8 @@ struct gw_ctx {
   void* flush_buf = nullptr;
   int fru_lanes = 4;        // lanes per FRU of the stage kernel: 1 or 4
   int stage_warps = 1;      // warps per block of the 4-lane stage kernels
+  int packed_warps = 0;     // > 0: packed stage launches of that many warps
+  uint32_t pack_launch = 0; // packed launches so far
   int precision = 0;        // 0: FP64, 1: mixed (FP32 rates and local ODE)
   double pca_scale = 1.0;   // LCC permeability scale of the cell
   gw_batch* batch = nullptr;  // set while the cell is a member of a batch

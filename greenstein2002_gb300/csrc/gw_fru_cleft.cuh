@@ -230,11 +230,13 @@ __device__ __forceinline__ void copy_row16(uint32_t* dst, const uint32_t* src, c
 // memory, and the global copy-on-twist rows of the first of them.
 struct StageCtx {
   const StageParams* p;
-  uint32_t* rows;         // 8 shared-memory rows, kMtSmemStride words apart
-  uint32_t* m;            // this lane's FRU row (one of rows)
-  uint32_t* hold0;        // copy-on-twist rows (global), FRU-major, of the warp's FRUs
-  uint32_t* hold_epoch0;  // their epochs
-  bool dirty;             // this FRU's staged words differ from its global row
+  uint32_t* rows;            // 8 shared-memory rows, kMtSmemStride words apart
+  uint32_t* m;               // this lane's FRU row (one of rows)
+  uint32_t* hold_base;       // copy-on-twist rows of the cell (global), FRU-major
+  uint32_t* hold_epoch_base; // their epochs
+  uint32_t* my_hold_epoch;   // the epoch of this lane's FRU
+  int f;                     // this lane's FRU (any value for a group without one)
+  bool dirty;                // this FRU's staged words differ from its global row
 };
 
 // The words of one substep are E_tot extra draws (lane c owns positions
@@ -264,12 +266,13 @@ __device__ __forceinline__ void regen_crossing(const StageCtx& sc, int lane, uns
     cross &= cross - 1u;
     const int gi = l0 >> 2;
     uint32_t* row = sc.rows + gi * kMtSmemStride;
+    const int fg = __shfl_sync(0xffffffffu, sc.f, l0);  // the FRU of group gi
     __syncwarp();  // group gi has read its old words
     if (copy & (1u << l0)) {
       const uint4* s4 = reinterpret_cast<const uint4*>(row);
-      uint4* d4 = reinterpret_cast<uint4*>(sc.hold0 + (size_t)gi * kMtStride);
+      uint4* d4 = reinterpret_cast<uint4*>(sc.hold_base + (size_t)fg * kMtStride);
       for (int i = lane; i < kMtN / 4; i += 32) d4[i] = s4[i];
-      if (lane == 0) sc.hold_epoch0[gi] = sc.p->epoch;
+      if (lane == 0) sc.hold_epoch_base[fg] = sc.p->epoch;
     }
     regen32(row, lane);
   }
@@ -366,246 +369,342 @@ __device__ __forceinline__ float frac_of(double t, double t0, double, float rint
   return (float)(t - t0) * rinterval;
 }
 
+// The constants of one lane for a stage (the same for every FRU of it).
+template <typename R>
+struct LaneStage {
+  R dep0[3], span[3], pca_scale, rinterval;
+  double t0, tf, interval;
+  // per-lane voltage exponential of the rates: alpha, beta, yCa_inf, tau_yCa
+  //   lane 0: alphacf*exp(0.012*(V-35))     lane 1: betacf*exp(-0.05*(V-35))
+  //   lane 2: 0.4/(1+exp((V+12.5)/5)) + 0.6  lane 3: 60 + 340/(1+exp((V+30)/12))
+  bool isdiv;
+  R cA, cR, cD, cCF, cK, cM;
+};
+
+template <typename R>
+__device__ __forceinline__ void lane_stage(const StageParams& p, const Group& g, LaneStage<R>& L) {
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    L.dep0[i] = (R)p.dep0[i];
+    L.span[i] = (R)p.span[i];
+  }
+  L.pca_scale = (R)p.pca_scale;
+  L.t0 = p.t0;
+  L.tf = p.tf;
+  L.interval = p.tf - p.t0;
+  L.rinterval = (R)(1.0 / L.interval);
+  L.isdiv = g.c >= 2;
+  L.cA = L.isdiv ? (g.c == 2 ? R(12.5) : R(30.0)) : R(-35.0);
+  L.cR = L.isdiv ? (g.c == 2 ? R(1.0 / 5.0) : R(1.0 / 12.0)) : (g.c == 0 ? R(0.012) : R(-0.05));
+  L.cD = L.isdiv ? (g.c == 2 ? R(5.0) : R(12.0)) : R(1.0);
+  L.cCF = L.isdiv ? R(0.0) : (g.c == 0 ? R(alphacf) : R(betacf));
+  L.cK = L.isdiv ? (g.c == 2 ? R(0.4) : R(340.0)) : R(1.0);
+  L.cM = L.isdiv ? (g.c == 2 ? R(1.0 - 0.4) : R(60.0)) : R(0.0);
+}
+
+// One FRU's state in the substep loop, as seen by one lane (its cleft):
+// the FP64 Ca state and clock, channel word, MT position, and the values
+// carried from one substep to the next.
+template <typename R>
+struct Fru4 {
+  double t, cajsr64, cass64;
+  uint32_t w, nsub;
+  int mti, nopen;
+  R dep[3], e2, a2j, lopen;
+  bool small;
+};
+
+// the FRU at the stage start (t0, voltages dep0)
+template <typename R>
+__device__ __forceinline__ void fru_begin(Fru4<R>& F, const LaneStage<R>& L) {
+#pragma unroll
+  for (int i = 0; i < 3; i++) F.dep[i] = L.dep0[i];
+  F.lopen = lcc_open(F.w) ? R(1) : R(0);
+  F.nopen = ryr_open_count(F.w);
+  F.t = L.t0;
+  ghk_terms(F.dep[0], L.pca_scale, F.e2, F.a2j, F.small);
+}
+
+// Values of one substep carried from its first half (rates, extra-draw
+// layout, words below 624) to its second (words past 624, Heun step,
+// transitions), between which the warp regenerates MT rows.
+template <typename R>
+struct Sub4 {
+  R cajsr, cass, alpha, beta, bp, gam, k12, k23, k34, k54, k25, k56, p34, R0[8];
+  int regime, ne, pre, etot;
+  uint32_t exw[kRyR], bw[8];
+};
+
+// First half of one substep of the FRU (simfru_local.c:83-146 up to the
+// draws): voltage terms, exit totals, the RyR constants, the layout of the
+// extra draws and the words that precede word 624.
+template <typename R>
+__device__ __forceinline__ void substep_a(Fru4<R>& F, Sub4<R>& S, const LaneStage<R>& L, const Group& g,
+                                          const StageCtx& sc) {
+  uint32_t& w = F.w;
+  const int mti = F.mti;
+  const R* dep = F.dep;
+  R &cajsr = S.cajsr, &cass = S.cass, &alpha = S.alpha, &beta = S.beta, &bp = S.bp, &gam = S.gam;
+  R &k12 = S.k12, &k23 = S.k23, &k34 = S.k34, &k54 = S.k54, &k25 = S.k25, &k56 = S.k56;
+  R* R0 = S.R0;
+  int &regime = S.regime, &ne = S.ne, &pre = S.pre, &etot = S.etot;
+  const bool isdiv = L.isdiv;
+  const R cA = L.cA, cR = L.cR, cD = L.cD, cCF = L.cCF, cK = L.cK, cM = L.cM;
+  cajsr = (R)F.cajsr64;
+  cass = (R)F.cass64;
+  // ---- voltage terms at the substep start, one exponential per lane ----
+  const R x = dep[0] + cA;
+  R q = x * cR;
+  if (isdiv) q = divc(x, cD, cR);
+  const R ev = rexp(q);
+  const R r01 = cCF * ev;
+  const R r23 = rdiv(cK, R(1) + ev) + cM;
+  const R vterm = isdiv ? r23 : r01;
+  alpha = from(g, vterm, 0);
+  beta = from(g, vterm, 1);
+  const R yinf = from(g, vterm, 2), tau = from(g, vterm, 3);
+  bp = divc(beta, R(bL * kappa), R(1.0 / (bL * kappa)));
+  const R ap = R(aL) * alpha;
+  // ---- exit totals of this cleft's 8 channels ----
+  gam = R(gammacf) * cass;
+  {
+    const int s = lcc_of(w);
+    const uint16_t bi = c_lcc_basis[s];
+    const R X = R(c_lcc_coef[s][0]) * pick_basis(bi & 15, alpha, beta, gam, ap, bp);
+    const R Y = R(c_lcc_coef[s][1]) * pick_basis((bi >> 4) & 15, alpha, beta, gam, ap, bp);
+    const R Z = R(c_lcc_coef[s][2]) * pick_basis((bi >> 8) & 15, alpha, beta, gam, ap, bp);
+    R0[0] = X + Y + Z;
+  }
+  {
+    const R num = (vdi_of(w) == 2) ? (R(1) - yinf) : yinf;
+    R0[1] = rdiv(num, tau);
+  }
+  // RyR constants of the cleft and the pseudo-state draws
+  const R c2 = cass * cass;
+  const R sat = imin(R(threshMAX), divc(c2, R(k_rate), R(1.0 / k_rate)));
+  const R sat2 = imin(R(threshMAX), divc(c2, R(k_rate2), R(1.0 / k_rate2)));
+  k12 = R(k12cf) * sat2;
+  k23 = R(k23cf) * sat;
+  k34 = R(k34cf) * sat;
+  k54 = R(k54cf) * sat;
+  k25 = R(k25cf) * sat;
+  k56 = R(k56cf) * sat;
+  {
+    const R cc = imin(cass, R(threshMAXCa));
+    regime = ilt(cc, R(threshCa56to8)) ? 0 : (ilt(cc, R(threshCa34to7)) ? 1 : 2);
+  }
+  // extra draws: regime 0 resolves 7 and 8, regime 1 resolves 7 (in cleft, then RyR order)
+  ne = 0;
+  #pragma unroll
+  for (int i = 0; i < kRyR; i++) {
+    const int s = ryr_of(w, i);
+    ne += (regime == 0 && (s == 7 || s == 8)) || (regime == 1 && s == 7);
+  }
+  const int n0 = from(g, ne, 0), n1 = from(g, ne, 1), n2 = from(g, ne, 2), n3 = from(g, ne, 3);
+  pre = (g.c > 0 ? n0 : 0) + (g.c > 1 ? n1 : 0) + (g.c > 2 ? n2 : 0);
+  etot = n0 + n1 + n2 + n3;
+  fetch_old(sc, g, mti, pre, ne, etot, S.exw, S.bw);
+}
+
+// Second half: the remaining words, the RyR pseudo-states, the substep size,
+// the Heun step of the local Ca ODE and the transitions (:135-277).
+template <typename R>
+__device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStage<R>& L, const Group& g,
+                                          StageCtx& sc) {
+  uint32_t& w = F.w;
+  int& mti = F.mti;
+  double& t = F.t;
+  R* dep = F.dep;
+  R &e2 = F.e2, &a2j = F.a2j, &lopen = F.lopen;
+  bool& small = F.small;
+  int& nopen = F.nopen;
+  const R cajsr = S.cajsr, cass = S.cass, alpha = S.alpha, beta = S.beta, bp = S.bp, gam = S.gam;
+  const R k12 = S.k12, k23 = S.k23, k34 = S.k34, k54 = S.k54, k25 = S.k25, k56 = S.k56;
+  R& p34 = S.p34;
+  R* R0 = S.R0;
+  const int regime = S.regime, ne = S.ne, pre = S.pre, etot = S.etot;
+  uint32_t* exw = S.exw;
+  uint32_t* bw = S.bw;
+  const R pca_scale = L.pca_scale;
+  fetch_new(sc, g, mti, pre, ne, etot, exw, bw);
+  {
+    // the draws are taken in order from a shifting window (static
+    // register indices); k34/(k34+k43) is formed once, for the draws of
+    // regimes 0/1 or for the merged state 7 of regime 2 (never both)
+    bool has7 = false, has34 = false;
+  #pragma unroll
+    for (int i = 0; i < kRyR; i++) {
+      const int s = ryr_of(w, i);
+      has7 |= (s == 7);
+      has34 |= (s == 3 || s == 4);
+    }
+    if ((regime <= 1 && has7) || (regime == 2 && (has7 || has34))) p34 = k34 / (k34 + R(k43));
+  #pragma unroll
+    for (int i = 0; i < kRyR; i++) {
+      int s = ryr_of(w, i);
+      if (regime == 0) {
+        if (s == 7 || s == 8) {
+          const uint32_t y = exw[0];
+          exw[0] = exw[1];
+          exw[1] = exw[2];
+          exw[2] = exw[3];
+          exw[3] = exw[4];
+          if (s == 7) s = u_below(y, p34) ? 4 : 3;
+          else s = u_below(y, k56 / (k56 + R(k65))) ? 6 : 5;
+        }
+      } else if (regime == 1) {
+        if (s == 7) {
+          const uint32_t y = exw[0];
+          exw[0] = exw[1];
+          exw[1] = exw[2];
+          exw[2] = exw[3];
+          exw[3] = exw[4];
+          s = u_below(y, p34) ? 4 : 3;
+        }
+        if (s == 5 || s == 6) s = 8;
+      } else {
+        if (s == 3 || s == 4) s = 7;
+        else if (s == 5 || s == 6) s = 8;
+      }
+      w = set_field(w, 8 + 4 * i, s);
+    }
+  }
+  {
+    bool need7 = false, need8 = false;
+  #pragma unroll
+    for (int i = 0; i < kRyR; i++) {
+      const int s = ryr_of(w, i);
+      need7 |= (s == 7);
+      need8 |= (s == 8);
+    }
+    const R T2 = R(k21) + k23 + k25, T3 = R(k32) + k34, T5 = R(k52) + k54 + k56;
+    const R T4 = R(k43 + k45);
+    R T7 = R(0), T8 = R(0);
+    if (need7) {
+      const R a1 = p34;  // k34 / (k43 + k34)
+      T7 = (R(1) - a1) * R(k32) + a1 * R(k45);
+    }
+    if (need8) {
+      const R a1 = R(k65) / (k56 + R(k65));
+      T8 = a1 * R(k52) + a1 * k54;
+    }
+  #pragma unroll
+    for (int i = 0; i < kRyR; i++) {
+      const int s = ryr_of(w, i);
+      R r = k12;
+      r = (s == 2) ? T2 : r;
+      r = (s == 3) ? T3 : r;
+      r = (s == 4) ? T4 : r;
+      r = (s == 5) ? T5 : r;
+      r = (s == 6) ? R(k65) : r;
+      r = (s == 7) ? T7 : r;
+      r = (s == 8) ? T8 : r;
+      R0[2 + i] = r;
+    }
+  }
+  R0[7] = (cl_of(w) == 1) ? R(kfIto2) * cass : R(kbIto2);
+  R mx = R(0);
+  #pragma unroll
+  for (int j = 0; j < 8; j++) mx = imax(mx, R0[j]);
+  mx = gmax(g, mx);
+  // ---- substep size (simfru_local.c:135-146) ----
+  R dtr = imin(rdiv(R(0.1), mx), R(10.001e-3));
+  const R cmax = gmax(g, imax(R(0.e-3), cass));
+  if (ilt(R(1.5e-3), cmax)) dtr = imin(dtr, R(5.001e-3));
+  const double dt64 = imin((double)dtr, L.tf - t);
+  const R dt = (R)dt64;
+  // ---- Heun step (simfru_local.c:149-173) ----
+  R dJ, dS;
+  fcn_fru4(g, cajsr, cass, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
+  const R k1J = dt * dJ, k1S = dt * dS;
+  const R y1J = cajsr + k1J, y1S = cass + k1S;
+  t = t + dt64;
+  const R frac = frac_of(t, L.t0, L.interval, L.rinterval);
+  #pragma unroll
+  for (int i = 0; i < 3; i++) dep[i] = L.dep0[i] + frac * L.span[i];
+  ghk_terms(dep[0], pca_scale, e2, a2j, small);
+  fcn_fru4(g, y1J, y1S, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
+  F.cajsr64 = F.cajsr64 + (double)((k1J + dt * dJ) / R(2));
+  F.cass64 = F.cass64 + (double)((k1S + dt * dS) / R(2));
+  // ---- transitions of this cleft's 8 channels (:215-276) ----
+  bool moved = false;
+  if (leave_gt(bw[0], dt, R0[0])) {
+    const LccBasisT<R> lb{alpha, beta, bp};
+    R r[4];
+    int d[4];
+    const int len = lcc_row(lcc_of(w), lb, gam, r, d);
+    w = set_field(w, 0, choose_dest(r, d, len, dt, bw[0]));
+  }
+  if (leave_ge(bw[1], dt, R0[1])) w = set_field(w, 4, 3 - vdi_of(w));
+  #pragma unroll
+  for (int i = 0; i < kRyR; i++) {
+    if (leave_gt(bw[2 + i], dt, R0[2 + i])) {
+      const RyrKT<R> k{k12, k23, k34, k54, k25, k56, regime};
+      R r[4];
+      int d[4];
+      const int len = ryr_row(ryr_of(w, i), k, r, d);
+      w = set_field(w, 8 + 4 * i, choose_dest(r, d, len, dt, bw[2 + i]));
+      moved = true;
+    }
+  }
+  if (leave_ge(bw[7], dt, R0[7])) w = set_field(w, 28, 3 - cl_of(w));
+  lopen = lcc_open(w) ? R(1) : R(0);
+  if (moved) nopen = ryr_open_count(w);
+  F.nsub++;
+}
+
+// Regenerate, with the whole warp, the MT rows whose draws in this substep
+// run past word 624 (`go`: this lane's FRU takes a substep now).
+template <typename R>
+__device__ __forceinline__ void regen_step(StageCtx& sc, int lane, const Group& g, bool go, const Fru4<R>& F,
+                                           const Sub4<R>& S) {
+  const bool cross = go && (F.mti + S.etot + 32 > kMtN);
+  const unsigned cross_mask = __ballot_sync(0xffffffffu, cross && g.c == 0);
+  const unsigned copy_mask = __ballot_sync(0xffffffffu, cross && g.c == 0 && *sc.my_hold_epoch != sc.p->epoch);
+  if (cross_mask) regen_crossing(sc, lane, cross_mask, copy_mask);
+  if (cross) sc.dirty = true;
+}
+
 // One FRU over [t0, tf] by its four lanes (simfru_local.c:83-277).  cajsr and
 // cass are the FRU's FP64 state; arithmetic runs in R.  Every lane of the
 // warp calls it together (live = false for a group without an FRU).
 template <typename R>
 __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live, double& cajsr64, double& cass64,
                                          uint32_t& w, int& mti, uint32_t& nsub, bool& overflow) {
-  const StageParams& p = *sc.p;
-  R dep0[3], span[3], dep[3];
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    dep0[i] = (R)p.dep0[i];
-    span[i] = (R)p.span[i];
-    dep[i] = dep0[i];
-  }
-  const R pca_scale = (R)p.pca_scale;
-  R lopen = lcc_open(w) ? R(1) : R(0);
-  int nopen = ryr_open_count(w);
-  const double interval = p.tf - p.t0;
-  const R rinterval = (R)(1.0 / interval);
-  double t = p.t0;
-  R e2, a2j;
-  bool small;
-  ghk_terms(dep[0], pca_scale, e2, a2j, small);
-  // per-lane voltage exponential of the rates: alpha, beta, yCa_inf, tau_yCa
-  //   lane 0: alphacf*exp(0.012*(V-35))     lane 1: betacf*exp(-0.05*(V-35))
-  //   lane 2: 0.4/(1+exp((V+12.5)/5)) + 0.6  lane 3: 60 + 340/(1+exp((V+30)/12))
-  const bool isdiv = g.c >= 2;
-  const R cA = isdiv ? (g.c == 2 ? R(12.5) : R(30.0)) : R(-35.0);
-  const R cR = isdiv ? (g.c == 2 ? R(1.0 / 5.0) : R(1.0 / 12.0)) : (g.c == 0 ? R(0.012) : R(-0.05));
-  const R cD = isdiv ? (g.c == 2 ? R(5.0) : R(12.0)) : R(1.0);
-  const R cCF = isdiv ? R(0.0) : (g.c == 0 ? R(alphacf) : R(betacf));
-  const R cK = isdiv ? (g.c == 2 ? R(0.4) : R(340.0)) : R(1.0);
-  const R cM = isdiv ? (g.c == 2 ? R(1.0 - 0.4) : R(60.0)) : R(0.0);
+  LaneStage<R> L;
+  lane_stage(*sc.p, g, L);
+  Fru4<R> F;
+  F.cajsr64 = cajsr64;
+  F.cass64 = cass64;
+  F.w = w;
+  F.mti = mti;
+  F.nsub = nsub;
+  fru_begin(F, L);
   const int lane = threadIdx.x & 31;
   while (true) {
     // all 32 lanes stay in the loop until every FRU of the warp is done, so
     // the warp can regenerate MT rows together; a group whose FRU has
     // reached tf (or never had one) idles
-    bool go = live && t < p.tf;
-    if (go && nsub >= (1u << 22)) {
+    bool go = live && F.t < L.tf;
+    if (go && F.nsub >= (1u << 22)) {
       overflow = true;
       go = false;
     }
     if (!__any_sync(0xffffffffu, go)) break;
-    R cajsr = R(0), cass = R(0), alpha = R(0), beta = R(0), bp = R(0), gam = R(0);
-    R k12 = R(0), k23 = R(0), k34 = R(0), k54 = R(0), k25 = R(0), k56 = R(0), p34 = R(0);
-    R R0[8];
-    int regime = 0, ne = 0, pre = 0, etot = 0;
-    uint32_t exw[kRyR] = {0u, 0u, 0u, 0u, 0u}, bw[8];
-    if (go) {
-      cajsr = (R)cajsr64;
-      cass = (R)cass64;
-      // ---- voltage terms at the substep start, one exponential per lane ----
-      const R x = dep[0] + cA;
-      R q = x * cR;
-      if (isdiv) q = divc(x, cD, cR);
-      const R ev = rexp(q);
-      const R r01 = cCF * ev;
-      const R r23 = rdiv(cK, R(1) + ev) + cM;
-      const R vterm = isdiv ? r23 : r01;
-      alpha = from(g, vterm, 0);
-      beta = from(g, vterm, 1);
-      const R yinf = from(g, vterm, 2), tau = from(g, vterm, 3);
-      bp = divc(beta, R(bL * kappa), R(1.0 / (bL * kappa)));
-      const R ap = R(aL) * alpha;
-      // ---- exit totals of this cleft's 8 channels ----
-      gam = R(gammacf) * cass;
-      {
-        const int s = lcc_of(w);
-        const uint16_t bi = c_lcc_basis[s];
-        const R X = R(c_lcc_coef[s][0]) * pick_basis(bi & 15, alpha, beta, gam, ap, bp);
-        const R Y = R(c_lcc_coef[s][1]) * pick_basis((bi >> 4) & 15, alpha, beta, gam, ap, bp);
-        const R Z = R(c_lcc_coef[s][2]) * pick_basis((bi >> 8) & 15, alpha, beta, gam, ap, bp);
-        R0[0] = X + Y + Z;
-      }
-      {
-        const R num = (vdi_of(w) == 2) ? (R(1) - yinf) : yinf;
-        R0[1] = rdiv(num, tau);
-      }
-      // RyR constants of the cleft and the pseudo-state draws
-      const R c2 = cass * cass;
-      const R sat = imin(R(threshMAX), divc(c2, R(k_rate), R(1.0 / k_rate)));
-      const R sat2 = imin(R(threshMAX), divc(c2, R(k_rate2), R(1.0 / k_rate2)));
-      k12 = R(k12cf) * sat2;
-      k23 = R(k23cf) * sat;
-      k34 = R(k34cf) * sat;
-      k54 = R(k54cf) * sat;
-      k25 = R(k25cf) * sat;
-      k56 = R(k56cf) * sat;
-      {
-        const R cc = imin(cass, R(threshMAXCa));
-        regime = ilt(cc, R(threshCa56to8)) ? 0 : (ilt(cc, R(threshCa34to7)) ? 1 : 2);
-      }
-      // extra draws: regime 0 resolves 7 and 8, regime 1 resolves 7 (in cleft, then RyR order)
-      ne = 0;
-  #pragma unroll
-      for (int i = 0; i < kRyR; i++) {
-        const int s = ryr_of(w, i);
-        ne += (regime == 0 && (s == 7 || s == 8)) || (regime == 1 && s == 7);
-      }
-      const int n0 = from(g, ne, 0), n1 = from(g, ne, 1), n2 = from(g, ne, 2), n3 = from(g, ne, 3);
-      pre = (g.c > 0 ? n0 : 0) + (g.c > 1 ? n1 : 0) + (g.c > 2 ? n2 : 0);
-      etot = n0 + n1 + n2 + n3;
-      fetch_old(sc, g, mti, pre, ne, etot, exw, bw);
-    }
-    // rows whose draws run past word 624 are regenerated by the whole warp
-    const bool cross = go && (mti + etot + 32 > kMtN);
-    const unsigned cross_mask = __ballot_sync(0xffffffffu, cross && g.c == 0);
-    const unsigned copy_mask =
-        __ballot_sync(0xffffffffu, cross && g.c == 0 && sc.hold_epoch0[lane >> 2] != p.epoch);
-    if (cross_mask) regen_crossing(sc, lane, cross_mask, copy_mask);
-    if (cross) sc.dirty = true;
-    if (go) {
-      fetch_new(sc, g, mti, pre, ne, etot, exw, bw);
-      {
-        // the draws are taken in order from a shifting window (static
-        // register indices); k34/(k34+k43) is formed once, for the draws of
-        // regimes 0/1 or for the merged state 7 of regime 2 (never both)
-        bool has7 = false, has34 = false;
-  #pragma unroll
-        for (int i = 0; i < kRyR; i++) {
-          const int s = ryr_of(w, i);
-          has7 |= (s == 7);
-          has34 |= (s == 3 || s == 4);
-        }
-        if ((regime <= 1 && has7) || (regime == 2 && (has7 || has34))) p34 = k34 / (k34 + R(k43));
-  #pragma unroll
-        for (int i = 0; i < kRyR; i++) {
-          int s = ryr_of(w, i);
-          if (regime == 0) {
-            if (s == 7 || s == 8) {
-              const uint32_t y = exw[0];
-              exw[0] = exw[1];
-              exw[1] = exw[2];
-              exw[2] = exw[3];
-              exw[3] = exw[4];
-              if (s == 7) s = u_below(y, p34) ? 4 : 3;
-              else s = u_below(y, k56 / (k56 + R(k65))) ? 6 : 5;
-            }
-          } else if (regime == 1) {
-            if (s == 7) {
-              const uint32_t y = exw[0];
-              exw[0] = exw[1];
-              exw[1] = exw[2];
-              exw[2] = exw[3];
-              exw[3] = exw[4];
-              s = u_below(y, p34) ? 4 : 3;
-            }
-            if (s == 5 || s == 6) s = 8;
-          } else {
-            if (s == 3 || s == 4) s = 7;
-            else if (s == 5 || s == 6) s = 8;
-          }
-          w = set_field(w, 8 + 4 * i, s);
-        }
-      }
-      {
-        bool need7 = false, need8 = false;
-  #pragma unroll
-        for (int i = 0; i < kRyR; i++) {
-          const int s = ryr_of(w, i);
-          need7 |= (s == 7);
-          need8 |= (s == 8);
-        }
-        const R T2 = R(k21) + k23 + k25, T3 = R(k32) + k34, T5 = R(k52) + k54 + k56;
-        const R T4 = R(k43 + k45);
-        R T7 = R(0), T8 = R(0);
-        if (need7) {
-          const R a1 = p34;  // k34 / (k43 + k34)
-          T7 = (R(1) - a1) * R(k32) + a1 * R(k45);
-        }
-        if (need8) {
-          const R a1 = R(k65) / (k56 + R(k65));
-          T8 = a1 * R(k52) + a1 * k54;
-        }
-  #pragma unroll
-        for (int i = 0; i < kRyR; i++) {
-          const int s = ryr_of(w, i);
-          R r = k12;
-          r = (s == 2) ? T2 : r;
-          r = (s == 3) ? T3 : r;
-          r = (s == 4) ? T4 : r;
-          r = (s == 5) ? T5 : r;
-          r = (s == 6) ? R(k65) : r;
-          r = (s == 7) ? T7 : r;
-          r = (s == 8) ? T8 : r;
-          R0[2 + i] = r;
-        }
-      }
-      R0[7] = (cl_of(w) == 1) ? R(kfIto2) * cass : R(kbIto2);
-      R mx = R(0);
-  #pragma unroll
-      for (int j = 0; j < 8; j++) mx = imax(mx, R0[j]);
-      mx = gmax(g, mx);
-      // ---- substep size (simfru_local.c:135-146) ----
-      R dtr = imin(rdiv(R(0.1), mx), R(10.001e-3));
-      const R cmax = gmax(g, imax(R(0.e-3), cass));
-      if (ilt(R(1.5e-3), cmax)) dtr = imin(dtr, R(5.001e-3));
-      const double dt64 = imin((double)dtr, p.tf - t);
-      const R dt = (R)dt64;
-      // ---- Heun step (simfru_local.c:149-173) ----
-      R dJ, dS;
-      fcn_fru4(g, cajsr, cass, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
-      const R k1J = dt * dJ, k1S = dt * dS;
-      const R y1J = cajsr + k1J, y1S = cass + k1S;
-      t = t + dt64;
-      const R frac = frac_of(t, p.t0, interval, rinterval);
-  #pragma unroll
-      for (int i = 0; i < 3; i++) dep[i] = dep0[i] + frac * span[i];
-      ghk_terms(dep[0], pca_scale, e2, a2j, small);
-      fcn_fru4(g, y1J, y1S, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
-      cajsr64 = cajsr64 + (double)((k1J + dt * dJ) / R(2));
-      cass64 = cass64 + (double)((k1S + dt * dS) / R(2));
-      // ---- transitions of this cleft's 8 channels (:215-276) ----
-      bool moved = false;
-      if (leave_gt(bw[0], dt, R0[0])) {
-        const LccBasisT<R> lb{alpha, beta, bp};
-        R r[4];
-        int d[4];
-        const int len = lcc_row(lcc_of(w), lb, gam, r, d);
-        w = set_field(w, 0, choose_dest(r, d, len, dt, bw[0]));
-      }
-      if (leave_ge(bw[1], dt, R0[1])) w = set_field(w, 4, 3 - vdi_of(w));
-  #pragma unroll
-      for (int i = 0; i < kRyR; i++) {
-        if (leave_gt(bw[2 + i], dt, R0[2 + i])) {
-          const RyrKT<R> k{k12, k23, k34, k54, k25, k56, regime};
-          R r[4];
-          int d[4];
-          const int len = ryr_row(ryr_of(w, i), k, r, d);
-          w = set_field(w, 8 + 4 * i, choose_dest(r, d, len, dt, bw[2 + i]));
-          moved = true;
-        }
-      }
-      if (leave_ge(bw[7], dt, R0[7])) w = set_field(w, 28, 3 - cl_of(w));
-      lopen = lcc_open(w) ? R(1) : R(0);
-      if (moved) nopen = ryr_open_count(w);
-      nsub++;
-    }
+    Sub4<R> S;
+    S.etot = 0;
+#pragma unroll
+    for (int i = 0; i < kRyR; i++) S.exw[i] = 0u;
+    S.p34 = R(0);
+    if (go) substep_a(F, S, L, g, sc);
+    regen_step(sc, lane, g, go, F, S);
+    if (go) substep_b(F, S, L, g, sc);
   }
+  cajsr64 = F.cajsr64;
+  cass64 = F.cass64;
+  w = F.w;
+  mti = F.mti;
+  nsub = F.nsub;
 }
 
 // Sum over the 32 lanes of a warp: one fixed shuffle tree.
@@ -706,6 +805,16 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
   const int lane = threadIdx.x & 31;
   const int grp = bidx * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
   const int ngroups = (s.nfru + 7) >> 3;
+  if ((p.flags & kFlagQueueReset) && bidx == 0 && threadIdx.x == 0) {
+    // after a packed launch: ready the queue for the next one (the heavy-FRU
+    // threshold becomes 3x this launch's mean substeps per FRU, at least 8)
+    const uint32_t n = (uint32_t)s.nfru;
+    const uint32_t thr = 3u * (s.qctl[3] / (n ? n : 1u));
+    s.qctl[4] = thr > 8u ? thr : 8u;
+    s.qctl[3] = 0u;
+    s.qctl[0] = 0u;
+    s.qctl[1 + ((p.launch + 1u) & 1u)] = 0u;
+  }
   if (grp >= ngroups) return;  // whole warps past the cell's last FRU
   if (s.trace_ns && lane == 0) s.trace_ns[2 * grp] = global_ns();
   Group g;
@@ -726,8 +835,10 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
   sc.p = &p;
   sc.rows = mt_stage + (threadIdx.x >> 5) * 8 * kMtSmemStride;
   sc.m = sc.rows + (lane >> 2) * kMtSmemStride;
-  sc.hold0 = s.mt_hold + (size_t)grp * 8 * kMtStride;
-  sc.hold_epoch0 = s.hold_epoch + grp * 8;
+  sc.hold_base = s.mt_hold;
+  sc.hold_epoch_base = s.hold_epoch;
+  sc.f = f;
+  sc.my_hold_epoch = s.hold_epoch + f;  // within the padded arrays even past the last FRU
   sc.dirty = false;
   bool restore = false;
   if (active) {
@@ -736,7 +847,7 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
       cass = s.frus_s[(g.c + 1) * nf + f];
       w = s.chan_s[g.c * nf + f];
       mti = s.mti_s[f];
-      restore = (sc.hold_epoch0[lane >> 2] == p.epoch);
+      restore = (*sc.my_hold_epoch == p.epoch);
     } else {
       cajsr = s.frus[f];
       cass = s.frus[(g.c + 1) * nf + f];
@@ -752,7 +863,7 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
       s.chan_s[g.c * nf + f] = w;
     }
   }
-  const uint32_t* hold = sc.hold0 + (size_t)(lane >> 2) * kMtStride;
+  const uint32_t* hold = sc.hold_base + (size_t)f * kMtStride;
   if (p.flags & kFlagAdvance) {
     // the FRUs' MT rows live in shared memory for the whole launch: every
     // draw and every regeneration is a shared-memory access
@@ -821,6 +932,152 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
 template <typename R>
 __device__ __forceinline__ void stage_body(const DevState& s, const StageParams& p, int bidx, double* out) {
   stage_body_fin<R>(s, p, bidx, OutFin{out});
+}
+
+// ---- packed stage: a queue of FRUs per 4-lane group -----------------------------
+// A warp's eight 4-lane groups each advance one FRU at a time and, when it
+// reaches tf, store it and take the next from the cell's queue, so a warp's
+// lanes stay busy until the queue is empty instead of idling behind the
+// slowest of eight fixed FRUs.  The queue hands out first the FRUs that were
+// heavy (many substeps) in the cell's previous packed launch, then the others
+// in order.  The per-FRU arithmetic is advance4's, so every FRU ends in the
+// same state as with the fixed layout; the flux sums come from a following
+// non-advancing launch over the stored states, in the usual fixed order.
+template <typename R>
+__device__ __forceinline__ void stage_body_packed(const DevState& s, const StageParams& p, double* out) {
+  extern __shared__ __align__(16) uint32_t mt_stage[];  // [warps][8][kMtSmemStride]
+  const int lane = threadIdx.x & 31;
+  Group g;
+  g.c = lane & 3;
+  g.base = lane & ~3;
+  g.mask = 0xfu << g.base;
+  const size_t nf = (size_t)s.stride;
+  const int n = s.nfru;
+  const uint32_t L = p.launch;
+  const int* heavy_prev = s.heavy_list + (size_t)((L + 1u) & 1u) * nf;
+  int* heavy_next = s.heavy_list + (size_t)(L & 1u) * nf;
+  // tags by launch parity too: this launch re-tags the FRUs it finds heavy
+  // without changing what its own queue skips
+  const uint32_t* tag_prev = s.heavy_tag + (size_t)((L + 1u) & 1u) * nf;
+  uint32_t* tag_next = s.heavy_tag + (size_t)(L & 1u) * nf;
+  const unsigned H = s.qctl[1 + ((L + 1u) & 1u)];
+  const unsigned thr = s.qctl[4];
+  LaneStage<R> LS;
+  lane_stage(p, g, LS);
+  StageCtx sc;
+  sc.p = &p;
+  sc.rows = mt_stage + (threadIdx.x >> 5) * 8 * kMtSmemStride;
+  sc.m = sc.rows + (lane >> 2) * kMtSmemStride;
+  sc.hold_base = s.mt_hold;
+  sc.hold_epoch_base = s.hold_epoch;
+  sc.f = 0;
+  sc.my_hold_epoch = s.hold_epoch;
+  sc.dirty = false;
+  Fru4<R> F;
+  F.t = 0.0;
+  F.cajsr64 = F.cass64 = 0.0;
+  F.w = 0u;
+  F.nsub = 0u;
+  F.mti = 0;
+  int f = -1;
+  bool overflow = false;
+  // the next FRU of the queue (every lane of the group gets it; -1: none left)
+  auto take = [&]() -> int {
+    int got = -1;
+    if (g.c == 0) {
+      for (int tries = 0; tries <= n + (int)H; tries++) {
+        const unsigned i = atomicAdd(s.qctl, 1u);
+        if (i < H) {
+          got = heavy_prev[i];
+          break;
+        }
+        const unsigned j = i - H;
+        if (j >= (unsigned)n) break;
+        if (H == 0u || tag_prev[j] != L) {  // tag L: in the previous launch's heavy list
+          got = (int)j;
+          break;
+        }
+      }
+    }
+    return __shfl_sync(g.mask, got, g.base);
+  };
+  auto load = [&](int ff) {
+    f = ff;
+    sc.f = ff;
+    sc.my_hold_epoch = s.hold_epoch + ff;
+    bool restore = false;
+    if (p.flags & kFlagResume) {
+      F.cajsr64 = s.frus_s[ff];
+      F.cass64 = s.frus_s[(g.c + 1) * nf + ff];
+      F.w = s.chan_s[g.c * nf + ff];
+      F.mti = s.mti_s[ff];
+      restore = (*sc.my_hold_epoch == p.epoch);
+    } else {
+      F.cajsr64 = s.frus[ff];
+      F.cass64 = s.frus[(g.c + 1) * nf + ff];
+      F.w = s.chan[g.c * nf + ff];
+      F.mti = s.mti[ff];
+    }
+    if (p.flags & kFlagSave) {
+      if (g.c == 0) {
+        s.frus_s[ff] = F.cajsr64;
+        s.mti_s[ff] = F.mti;
+      }
+      s.frus_s[(g.c + 1) * nf + ff] = F.cass64;
+      s.chan_s[g.c * nf + ff] = F.w;
+    }
+    copy_row16(sc.m, restore ? s.mt_hold + (size_t)ff * kMtStride : s.mt + (size_t)ff * kMtStride, g);
+    sc.dirty = restore;
+    F.nsub = 0u;
+    fru_begin(F, LS);
+  };
+  auto finish = [&]() {
+    if (sc.dirty) copy_row16(s.mt + (size_t)f * kMtStride, sc.m, g);
+    if (g.c == 0) {
+      s.frus[f] = F.cajsr64;
+      s.mti[f] = F.mti;
+      if (s.trace_sub) s.trace_sub[f] = F.nsub;
+      atomicAdd(&s.qctl[3], F.nsub);
+      if (s.substeps) atomicAdd(s.substeps, (unsigned long long)F.nsub);
+      if (F.nsub >= thr && thr > 0u) {
+        tag_next[f] = L + 1u;
+        heavy_next[atomicAdd(&s.qctl[1 + (L & 1u)], 1u)] = f;
+      }
+    }
+    s.frus[(g.c + 1) * nf + f] = F.cass64;
+    s.chan[g.c * nf + f] = F.w;
+  };
+  {
+    const int ff = take();
+    if (ff >= 0) load(ff);
+  }
+  __syncwarp();
+  while (true) {
+    const bool has = f >= 0;
+    bool go = has && F.t < LS.tf;
+    if (go && F.nsub >= (1u << 22)) {
+      overflow = true;
+      go = false;
+    }
+    if (!__any_sync(0xffffffffu, has)) break;
+    Sub4<R> S;
+    S.etot = 0;
+#pragma unroll
+    for (int i = 0; i < kRyR; i++) S.exw[i] = 0u;
+    S.p34 = R(0);
+    if (go) substep_a(F, S, LS, g, sc);
+    regen_step(sc, lane, g, go, F, S);
+    if (go) substep_b(F, S, LS, g, sc);
+    // a group whose FRU reached tf stores it and takes the next one
+    if (has && !(go && F.t < LS.tf)) {
+      finish();
+      f = -1;
+      const int ff = take();
+      if (ff >= 0) load(ff);
+    }
+    __syncwarp();
+  }
+  if (overflow) out[kOutError] = 1.0;
 }
 
 // ---- many cells in one launch ------------------------------------------------

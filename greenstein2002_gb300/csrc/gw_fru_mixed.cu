@@ -30,4 +30,15 @@ cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, int warps,
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(32) fru_stage_mixed_packed_kernel(DevState s, StageParams p) {
+  cleft::stage_body_packed<float>(s, p, s.out);
+}
+
+cudaError_t launch_stage_mixed_packed(const DevState& s, const StageParams& p, int warps, cudaStream_t st) {
+  static const cudaError_t attr = stage_smem_attributes(fru_stage_mixed_packed_kernel);
+  if (attr != cudaSuccess) return attr;
+  fru_stage_mixed_packed_kernel<<<warps, 32, kStageSmemPerWarp, st>>>(s, p);
+  return cudaGetLastError();
+}
+
 }  // namespace gw

@@ -28,4 +28,15 @@ cudaError_t launch_stage4_batch(const BatchArgs& a, int nblocks, int warps, cuda
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(32) fru_stage4_packed_kernel(DevState s, StageParams p) {
+  cleft::stage_body_packed<double>(s, p, s.out);
+}
+
+cudaError_t launch_stage4_packed(const DevState& s, const StageParams& p, int warps, cudaStream_t st) {
+  static const cudaError_t attr = stage_smem_attributes(fru_stage4_packed_kernel);
+  if (attr != cudaSuccess) return attr;
+  fru_stage4_packed_kernel<<<warps, 32, kStageSmemPerWarp, st>>>(s, p);
+  return cudaGetLastError();
+}
+
 }  // namespace gw

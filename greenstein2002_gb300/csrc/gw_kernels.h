@@ -37,6 +37,7 @@ enum : int {
   kFlagSave = 2,     // snapshot FRU state before advancing (send_save_state)
   kFlagResume = 4,   // restore the snapshot before advancing (send_resume_state)
   kFlagAvg = 8,      // also reduce the 11 output-average sums (calc_fru_avg_local)
+  kFlagQueueReset = 16,  // reset the FRU queue of the packed kernel for its next launch
 };
 enum : int { kSeedBase = 0, kSeedReference = 1 };
 
@@ -69,6 +70,13 @@ struct DevState {
   // 4-lane launch, and each 8-FRU warp's begin/end global time (ns)
   uint32_t* trace_sub;
   unsigned long long* trace_ns;
+  // FRU queue of the packed stage kernel: qctl[0] queue head, [1..2] counts
+  // of the heavy-FRU lists by launch parity, [3] substeps of the launch,
+  // [4] heavy threshold; heavy_list[2][stride]; heavy_tag[2][stride] = the
+  // packed launch + 1 in which the FRU was last heavy (by launch parity)
+  unsigned* qctl;
+  int* heavy_list;
+  uint32_t* heavy_tag;
 };
 
 struct StageParams {
@@ -78,6 +86,7 @@ struct StageParams {
   double pca_scale;  // LCC permeability scale of the cell (1 = reference PCa)
   uint32_t epoch;
   int flags;
+  uint32_t launch;  // packed launches of the cell so far
 };
 
 // Many cells in one launch (cleft-parallel kernels): cell i owns blocks
@@ -101,6 +110,12 @@ cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, int warps,
 // local ODE)
 cudaError_t launch_stage4(const DevState& s, const StageParams& p, int warps, cudaStream_t st);
 cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, int warps, cudaStream_t st);
+// packed variants: `warps` single-warp blocks whose 4-lane groups take the
+// cell's FRUs from a queue (heaviest of the previous launch first); they
+// advance and store the FRUs only -- the sums come from a following
+// non-advancing launch with kFlagQueueReset
+cudaError_t launch_stage4_packed(const DevState& s, const StageParams& p, int warps, cudaStream_t st);
+cudaError_t launch_stage_mixed_packed(const DevState& s, const StageParams& p, int warps, cudaStream_t st);
 cudaError_t launch_avg(const DevState& s, cudaStream_t st);
 // FP64 FMA throughput of the device (TFLOP/s, best of a few launches).
 cudaError_t probe_fp64(int sms, double* tflops);

@@ -10,7 +10,10 @@
 // the state and keeps the fastest candidate.  Candidates:
 //   - 4 lanes per FRU (8 FRUs per warp) with 1, 2, 4 or 8 warps per block;
 //   - 1 lane per FRU (32 FRUs per warp), FP64 cells with the reference PCa
-//     only, single-cell or per-stream runs only.
+//     only, single-cell or per-stream runs only;
+//   - packed launches (4 lanes per FRU, FRUs taken from a queue) with a half,
+//     a quarter or an eighth as many warps as the cell has 8-FRU groups (16,
+//     32 or 64 FRUs per warp on average), not in a batch.
 // Every candidate computes the same bits (per-FRU arithmetic is the same and
 // the flux sums use one fixed order), so tuning never changes a result.
 #include <cuda_runtime.h>
@@ -72,17 +75,23 @@ extern "C" int gw_autotune(int n, gw_ctx** cells, const gw_settings* sets, const
     one_lane_ok = one_lane_ok && cells[i]->precision == 0 && cells[i]->pca_scale == 1.0;
   }
   std::vector<Saved> saved(n);
-  std::vector<int> lanes0(n), warps0(n);
+  std::vector<int> lanes0(n), warps0(n), pack0(n);
   for (int i = 0; i < n; i++) {
     int rc = save_cell(cells[i], saved[i]);
     if (rc) return rc;
     lanes0[i] = cells[i]->fru_lanes;
     warps0[i] = cells[i]->stage_warps;
+    pack0[i] = cells[i]->packed_warps;
   }
   struct Cand {
-    int lanes, warps;
+    int lanes, warps, pack_div;  // pack_div > 0: packed, groups / pack_div warps
   };
-  const Cand cands[GW_TUNE_CANDIDATES] = {{4, 1}, {4, 2}, {4, 4}, {4, 8}, {1, 1}};
+  const Cand cands[GW_TUNE_CANDIDATES] = {{4, 1, 0}, {4, 2, 0}, {4, 4, 0}, {4, 8, 0},
+                                          {1, 1, 0}, {4, 1, 2}, {4, 1, 4}, {4, 1, 8}};
+  auto pack_warps = [&](int i, const Cand& k) {
+    const int groups = (gw_nfru(cells[i]) + 7) / 8;
+    return k.pack_div ? (groups + k.pack_div - 1) / k.pack_div : 0;
+  };
   double best = 1e300;
   int best_i = 0, rc = GW_OK;
   std::vector<double> tt(n), st(37 * (size_t)n), os(n);
@@ -90,10 +99,12 @@ extern "C" int gw_autotune(int n, gw_ctx** cells, const gw_settings* sets, const
   for (int k = 0; k < GW_TUNE_CANDIDATES; k++) {
     if (ms_out) ms_out[k] = -1.0;
     if (cands[k].lanes == 1 && !one_lane_ok) continue;
+    if (cands[k].pack_div && batch) continue;
     for (int i = 0; i < n && !rc; i++) {
       rc = restore_cell(cells[i], saved[i]);
       if (!rc) rc = gw_set_fru_lanes(cells[i], cands[k].lanes);
       if (!rc) rc = gw_set_stage_warps(cells[i], cands[k].warps);
+      if (!rc) rc = gw_set_stage_packing(cells[i], pack_warps(i, cands[k]));
     }
     if (!rc && batch) rc = gw_batch_set_warps(batch, cands[k].warps);
     if (rc) break;
@@ -121,6 +132,7 @@ extern "C" int gw_autotune(int n, gw_ctx** cells, const gw_settings* sets, const
     int r2 = restore_cell(cells[i], saved[i]);
     if (!r2) r2 = gw_set_fru_lanes(cells[i], rc ? lanes0[i] : cands[best_i].lanes);
     if (!r2) r2 = gw_set_stage_warps(cells[i], rc ? warps0[i] : cands[best_i].warps);
+    if (!r2) r2 = gw_set_stage_packing(cells[i], rc ? pack0[i] : pack_warps(i, cands[best_i]));
     if (!rc) rc = r2;
   }
   if (batch) {
@@ -129,6 +141,6 @@ extern "C" int gw_autotune(int n, gw_ctx** cells, const gw_settings* sets, const
   }
   if (rc) return rc;
   if (lanes_out) *lanes_out = cands[best_i].lanes;
-  if (warps_out) *warps_out = cands[best_i].warps;
+  if (warps_out) *warps_out = cands[best_i].pack_div ? -cands[best_i].pack_div : cands[best_i].warps;
   return GW_OK;
 }

@@ -91,6 +91,13 @@ int gw_set_fru_lanes(gw_ctx *ctx, int lanes);
 /* Warps per block of the 4-lane stage kernels: 1 (default), 2, 4 or 8.  A
  * launch-shape choice only; every value gives the same results. */
 int gw_set_stage_warps(gw_ctx *ctx, int warps);
+/* Packed stage launches (0 = off, the default): `warps` warps whose 4-lane
+ * groups take the cell's FRUs from a queue -- the heaviest of the previous
+ * launch first -- until none are left, instead of 8 fixed FRUs per warp
+ * (so FRUs per warp = 8 x FRUs / (8 x warps) on average).  A launch-shape
+ * choice only: every FRU ends in the same state and the flux sums keep
+ * their order. */
+int gw_set_stage_packing(gw_ctx *ctx, int warps);
 
 /* Arithmetic of the FRU path: 0 (default) = FP64, the plain method;
  * 1 = mixed precision: transition rates and the FRU-local Ca ODE in FP32,
@@ -237,15 +244,18 @@ int gw_batch_set_warps(gw_batch *batch, int warps);
 
 /* Autotuner (no reference counterpart): runs window_ms of the cells' own
  * workload from their current state once per stage-kernel launch shape --
- * 4 lanes per FRU with 1, 2, 4 or 8 warps per block, and 1 lane per FRU
- * (FP64 cells with the reference PCa, not in a batch) -- then restores
- * their state and sets the fastest shape on every cell (and on the batch).
+ * 4 lanes per FRU with 1, 2, 4 or 8 warps per block, 1 lane per FRU (FP64
+ * cells with the reference PCa, not in a batch), and packed launches with
+ * a half, a quarter or an eighth as many warps as the cell has 8-FRU groups
+ * (not in a batch) -- then restores their state and sets the fastest shape
+ * on every cell (and on the batch).  *warps receives the warps per block,
+ * or -2 / -4 / -8 for the packed shapes.
  * The cells run alone (n = 1), concurrently on their own streams (batch
  * NULL) or through the batch.  t, states [n][37] and oldsteps are read, not
  * advanced.  ms (may be NULL) receives the wall time of each of the
  * GW_TUNE_CANDIDATES candidates in the order above, -1 where not run.
  * Results never depend on the shape chosen. */
-#define GW_TUNE_CANDIDATES 5
+#define GW_TUNE_CANDIDATES 8
 int gw_autotune(int n, gw_ctx **cells, const gw_settings *sets, const double *t, const double *states,
                 const double *oldsteps, double window_ms, gw_batch *batch, int *lanes, int *warps, double *ms);
 

@@ -1,6 +1,7 @@
 """Launch shapes and the autotuner (gw_autotune): every stage-kernel shape --
-1 or 4 lanes per FRU, 1 to 8 warps per block, alone or batched -- gives the
-same bits, and tuning leaves the cells' state as it found it."""
+1 or 4 lanes per FRU, 1 to 8 warps per block, packed launches that take FRUs
+from a queue, alone or batched -- gives the same bits, and tuning leaves the
+cells' state as it found it."""
 import numpy as np
 import pytest
 
@@ -16,7 +17,10 @@ def _run_shape(gw, prec, lanes, warps, n=500):
     c = cells[0]
     if lanes == 1:
         c.set_fru_lanes(1)
-    c.set_stage_warps(warps)
+    if warps < 0:  # packed: a 1/|warps| share of the 8-FRU groups as warps
+        c.set_stage_packing(((n + 7) // 8 + (-warps) - 1) // (-warps))
+    else:
+        c.set_stage_warps(warps)
     st = states[0].copy()
     _, tr, ot, cu = c.run(st, 0.0, STEPS, set_=sets[0])
     return tr, ot, cu, c.download()
@@ -24,7 +28,7 @@ def _run_shape(gw, prec, lanes, warps, n=500):
 
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_all_shapes_same_bits(gw, prec):
-    shapes = [(4, 1), (4, 2), (4, 4), (4, 8)] + ([(1, 1)] if prec == "fp64" else [])
+    shapes = [(4, 1), (4, 2), (4, 4), (4, 8), (4, -2), (4, -4), (4, -16)] + ([(1, 1)] if prec == "fp64" else [])
     ref = _run_shape(gw, prec, *shapes[0])
     for lanes, warps in shapes[1:]:
         got = _run_shape(gw, prec, lanes, warps)
@@ -60,7 +64,7 @@ def test_autotune_restores_state(gw, mode):
     batch = gw.Batch(prec) if mode == "lockstep" else None
     lanes, warps, ms = gw.autotune(cells, sets, t, states, old, 2.0, batch=batch)
     assert (lanes, warps) in gw.TUNE_CANDIDATES and (lanes, warps) in ms
-    assert len(ms) == (5 if mode == "single" else 4)
+    assert len(ms) == {"single": 8, "streams": 7, "lockstep": 4}[mode]
     assert ms[(lanes, warps)] == min(ms.values())
     for c, b0 in zip(cells, before):
         got = c.download()
