@@ -87,6 +87,8 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-devdp", action="store_true", help="skip the device-integrator batched run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--packed", type=int, default=0,
+                    help="force packed launches with 1/N as many warps as 8-FRU groups (no autotuning)")
     ap.add_argument("--tune-ms", type=float, default=2.0, help="simulated window per autotuner candidate")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[1.0, 10.0, 50.0, 200.0])
     ap.add_argument("--serve-requests", type=int, default=48,
@@ -310,6 +312,24 @@ def tune_summary(res, args):
             "candidates_ms": {_shape_name(k): round(v, 2) for k, v in sorted(ms.items())}}
 
 
+def choose_shape(G, args, cells, sets, t, states, old):
+    """The launch shape of a timed section: forced packed (--packed N), the
+    default (--no-autotune), or the autotuner's choice on the section's own
+    workload."""
+    import numpy as np
+    if args.packed:
+        tuning = {"lanes_per_fru": 4, "fru_per_warp": 8 * args.packed, "warps_per_block": 1,
+                  "packed_div": args.packed, "forced": True}
+        for c in cells:
+            apply_tuning(c, tuning)
+        return tuning
+    if args.no_autotune or args.fru_lanes != 4:
+        return None
+    return tune_summary(G.autotune(cells, sets, np.ascontiguousarray(t, dtype=np.float64),
+                                   np.ascontiguousarray(states), np.ascontiguousarray(old, dtype=np.float64),
+                                   args.tune_ms), args)
+
+
 def apply_tuning(cell, tuning):
     """Give another cell the shape the autotuner chose (results never depend on it)."""
     cell.set_fru_lanes(tuning["lanes_per_fru"])
@@ -329,10 +349,8 @@ def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
     for _ in range(args.warmup):
         t, _, _, _ = cell.run(state, t, n, oldstep, st, want=())
         oldstep = cell.oldstep
-    tuning = None
-    if not args.no_autotune and args.fru_lanes == 4:
-        # launch shape picked on this cell's own workload (same results either way)
-        tuning = tune_summary(G.autotune([cell], [st], [t], state[None, :], [oldstep], args.tune_ms), args)
+    # launch shape picked on this cell's own workload (same results either way)
+    tuning = choose_shape(G, args, [cell], [st], np.array([t]), state[None, :].copy(), np.array([oldstep]))
     sub0, launch0 = cell.substeps(), cell.launches()
     cell.profile(True)
     total_ms = 0.0
@@ -391,9 +409,7 @@ def time_ensemble(G, args, dist, precision, clocks=None):
     step = int(args.step_ms)
     for _ in range(args.warmup):
         runner.run(cells, sets, t, states, old, step, lockstep=False)
-    tuning = None
-    if not args.no_autotune and args.fru_lanes == 4:
-        tuning = tune_summary(G.autotune(cells, sets, t, states, old, args.tune_ms), args)
+    tuning = choose_shape(G, args, cells, sets, t, states, old)
     sub0 = sum(c.substeps() for c in cells)
     launch0 = sum(c.launches() for c in cells)
     timer = G.GroupTimer(cells)
