@@ -133,3 +133,9 @@ int gw_avg_sums(gw_ctx *c, double num[11])
 int gw_save(gw_ctx *c) { copy_set(&c->saved, &c->live, c->n); return GW_OK; }
 int gw_resume(gw_ctx *c) { copy_set(&c->live, &c->saved, c->n); return GW_OK; }
 int gw_substeps(gw_ctx *c, unsigned long long *n) { *n = c->substeps; return GW_OK; }
+/* launch-shape and precision settings: the stand-in has one shape and FP64 only */
+int gw_set_fru_lanes(gw_ctx *c, int lanes) { (void)c; return lanes == 1 || lanes == 4 ? GW_OK : GW_EINVAL; }
+int gw_set_stage_warps(gw_ctx *c, int warps) { (void)c; return warps >= 1 && warps <= 8 ? GW_OK : GW_EINVAL; }
+int gw_set_stage_packing(gw_ctx *c, int warps) { (void)c; return warps >= 0 ? GW_OK : GW_EINVAL; }
+int gw_set_precision(gw_ctx *c, int precision) { (void)c; return precision == 0 ? GW_OK : GW_EINVAL; }
+int gw_set_pca_scale(gw_ctx *c, double scale) { (void)c; return scale == 1.0 ? GW_OK : GW_EINVAL; }

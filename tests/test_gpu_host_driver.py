@@ -16,3 +16,22 @@ def test_gpu_exact_restart_continues_bit_for_bit(gw, tmp_path):
     assert os.path.isfile(exe), "gw_caf not built"
     written = exact_restart_case(exe, tmp_path)
     assert "fruprops_4.1.txt" in written and "fruprops_avg_tot.1.txt" in written
+
+
+def test_gpu_launch_shapes_same_files(gw, tmp_path):
+    """The host driver's output files do not depend on the stage kernels'
+    launch shape (fixed 8 FRUs per warp, 4-warp blocks, packed queue), through
+    the integrator's saves, rejections and resumes."""
+    import filecmp
+    import subprocess
+    exe = os.path.join(ROOT, "greenstein2002_gb300", "_build", "gw_caf")
+    base = {"NFRU_sim": 500, "time_end": 14.0, "ic_file_flag": 0, "seed_scheme": 0, "seed_base": 5489}
+    runs = {"fixed": {}, "warps4": {"stage_warps": 4}, "packed4": {"stage_packing": 4}}
+    for name, extra in runs.items():
+        d = tmp_path / name
+        d.mkdir()
+        subprocess.run([exe] + ["%s=%s" % kv for kv in dict(base, **extra).items()], cwd=d, check=True,
+                       capture_output=True)
+    for name in ("warps4", "packed4"):
+        for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
+            assert filecmp.cmp(tmp_path / "fixed" / f, tmp_path / name / f, shallow=False), (name, f)
