@@ -5,9 +5,9 @@
 
 namespace gw {
 
-// One warp per block: a 12,500-FRU cell is 391 warps, fewer than the 608
-// SM sub-partitions of a GB300, so single-warp blocks spread them over all
-// 152 SMs instead of leaving SMs idle.
+// Block size of the one-thread-per-FRU kernels (fru_stage_kernel, the
+// average and seeding kernels): one warp per block, so a 12,500-FRU cell's
+// 391 warps spread over all 152 SMs instead of filling a few.
 constexpr int kStageThreads = 32;
 // Cleft-parallel stage kernels: 8 FRUs per warp, 1 .. kMaxStageWarps warps
 // per block (a launch-shape choice only: the results are the same bits).
