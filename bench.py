@@ -86,6 +86,9 @@ def parse():
                     help="streams: each cell on its own stream; lockstep: shared batched launches")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-devdp", action="store_true", help="skip the device-integrator batched run")
+    ap.add_argument("--precision-ensemble", type=int, nargs=2, metavar=("SEEDS", "MS"), default=None,
+                    help="only run the mixed-vs-FP64 ensemble check: SEEDS 12,500-FRU cells per precision "
+                         "over [0, MS) ms, APD90 / peak Cai / JSR depletion / open probabilities")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--packed", type=int, default=0,
                     help="force packed launches with 1/N as many warps as 8-FRU groups (no autotuning)")
@@ -637,12 +640,81 @@ def time_serving(G, args, rate):
             "cell_ms_per_s": cell_ms / wall, "cell_ms_per_s_12500_equiv": eq / wall}
 
 
+def apd90(t_ms, v):
+    """Action-potential duration at 90% repolarisation of the first beat (from
+    the upstroke's crossing of the 90% level to the repolarisation's)."""
+    import numpy as np
+    i0 = int(np.argmax(v))
+    vmax, vrest = v[i0], v[0]
+    thr = vmax - 0.9 * (vmax - vrest)
+    up = int(np.argmax(v > thr))
+    after = np.nonzero(v[i0:] < thr)[0]
+    return float(t_ms[i0 + after[0]] - t_ms[up]) if len(after) else float("nan")
+
+
+def precision_ensemble(G, args, dist):
+    """Mixed precision against the FP64 GPU oracle on full-size cells: SEEDS
+    12,500-FRU cells per precision, cell k's FRU j seeded 5489 + 100000 k + j,
+    from rest through the first beat; per seed APD90 and peak Cai, and the
+    ensemble's JSR depletion and LCC / RyR open-probability traces."""
+    import numpy as np
+    seeds, ms = args.precision_ensemble
+    t_ms = np.arange(1, ms + 1, dtype=float)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        cells, sets, states = [], [], []
+        for k in range(seeds):
+            c = G.Cell(NFRU, precision=prec)
+            if prec == "fp64":
+                c.set_stage_packing(((NFRU + 7) // 8 + 3) // 4)  # the FP64 ensemble's tuned shape
+            st = G.settings()
+            states.append(c.init_rest(st, scheme=G.SEED_BASE, base=SEED + 100000 * k))
+            cells.append(c)
+            sets.append(st)
+        states = np.ascontiguousarray(np.array(states))
+        runner = G.Batch(prec)
+        t0 = time.perf_counter()
+        st_tr, ot_tr = runner.run(cells, sets, np.zeros(seeds), states, np.full(seeds, 0.1), ms, traces=True,
+                                  lockstep=False)
+        wall = time.perf_counter() - t0
+        for c in cells:
+            c.close()
+        runner.close()
+        res[prec] = {"apd90": np.array([apd90(t_ms, v) for v in st_tr[:, :, 0]]), "peak_cai": st_tr[:, :, 6].max(1),
+                     "jsr": ot_tr[:, :, 1].mean(0), "plcc": ot_tr[:, :, 7].mean(0), "pryr": ot_tr[:, :, 3].mean(0),
+                     "wall_s": wall}
+    f, m = res["fp64"], res["mixed"]
+    d_apd = m["apd90"] - f["apd90"]
+    d_pk = m["peak_cai"] - f["peak_cai"]
+    ok = ~np.isnan(d_apd)
+    return {"check": "precision_ensemble", "seeds": seeds, "window_ms": [0, ms], "nfru": NFRU,
+            "apd90_ms": {"fp64_mean": float(np.nanmean(f["apd90"])), "mixed_mean": float(np.nanmean(m["apd90"])),
+                         "rel_diff_of_means": float(np.nanmean(m["apd90"]) / np.nanmean(f["apd90"]) - 1.0),
+                         "paired_sem_rel": float(np.std(d_apd[ok], ddof=1) / np.sqrt(ok.sum()) / np.nanmean(f["apd90"])),
+                         "seeds_repolarised": int(ok.sum())},
+            "peak_cai_mM": {"fp64_mean": float(f["peak_cai"].mean()), "mixed_mean": float(m["peak_cai"].mean()),
+                            "rel_diff_of_means": float(m["peak_cai"].mean() / f["peak_cai"].mean() - 1.0),
+                            "paired_sem_rel": float(np.std(d_pk, ddof=1) / np.sqrt(seeds) / f["peak_cai"].mean())},
+            "jsr_depletion": {"fp64_min_mean_cajsr_mM": float(f["jsr"].min()), "mixed_min_mean_cajsr_mM": float(m["jsr"].min()),
+                              "rel_diff": float(m["jsr"].min() / f["jsr"].min() - 1.0)},
+            "open_probability_traces": {"max_abs_diff_lcc": float(np.max(np.abs(m["plcc"] - f["plcc"]))),
+                                        "max_lcc": float(np.max(f["plcc"])),
+                                        "max_abs_diff_ryr": float(np.max(np.abs(m["pryr"] - f["pryr"]))),
+                                        "max_ryr": float(np.max(f["pryr"]))},
+            "wall_s": {"fp64": f["wall_s"], "mixed": m["wall_s"]}}
+
+
 def run_gpu(args, dist):
     import numpy as np
     import greenstein2002_gb300 as G
     from greenstein2002_gb300 import build as gb
     gb.build()
     G.load()
+    if args.precision_ensemble:
+        res = precision_ensemble(G, args, dist)
+        if dist.rank == 0:
+            print(json.dumps(res))
+        return
     seed = SEED + dist.rank * args.nfru  # replicas: independent streams per rank
     clocks = Clocks(dist.local)
     # headline: the FP64 ensemble, all cells on the GPU at once
