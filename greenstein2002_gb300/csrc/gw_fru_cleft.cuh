@@ -402,12 +402,44 @@ __device__ __forceinline__ void lane_stage(const StageParams& p, const Group& g,
   L.cM = L.isdiv ? (g.c == 2 ? R(1.0 - 0.4) : R(60.0)) : R(0.0);
 }
 
+// Accumulator of an FRU Ca concentration over the substeps.  FP64: a double,
+// updated as the reference does.  Mixed precision: a compensated FP32 pair
+// (Neumaier's summation: hi + lo carries about 48 bits), so the FP32
+// increments accumulate without FP64 instructions or conversions in the
+// substep loop; the FRU arrays stay FP64 (split on load, joined on store).
+template <typename R>
+struct CaAcc;
+template <>
+struct CaAcc<double> {
+  double v;
+  __device__ __forceinline__ void set(double x) { v = x; }
+  __device__ __forceinline__ double get() const { return v; }
+  __device__ __forceinline__ double r() const { return v; }
+  __device__ __forceinline__ void add(double inc) { v = v + inc; }
+};
+template <>
+struct CaAcc<float> {
+  float hi, lo;
+  __device__ __forceinline__ void set(double x) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+  }
+  __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ float r() const { return hi + lo; }
+  __device__ __forceinline__ void add(float inc) {
+    const float t = hi + inc;
+    lo = lo + ((fabsf(hi) >= fabsf(inc)) ? (hi - t) + inc : (inc - t) + hi);
+    hi = t;
+  }
+};
+
 // One FRU's state in the substep loop, as seen by one lane (its cleft):
 // the FP64 Ca state and clock, channel word, MT position, and the values
 // carried from one substep to the next.
 template <typename R>
 struct Fru4 {
-  double t, cajsr64, cass64;
+  double t;
+  CaAcc<R> jsr, ss;  // CaJSR and this cleft's CaSS
   uint32_t w, nsub;
   int mti, nopen;
   R dep[3], e2, a2j, lopen;
@@ -450,8 +482,8 @@ __device__ __forceinline__ void substep_a(Fru4<R>& F, Sub4<R>& S, const LaneStag
   int &regime = S.regime, &ne = S.ne, &pre = S.pre, &etot = S.etot;
   const bool isdiv = L.isdiv;
   const R cA = L.cA, cR = L.cR, cD = L.cD, cCF = L.cCF, cK = L.cK, cM = L.cM;
-  cajsr = (R)F.cajsr64;
-  cass = (R)F.cass64;
+  cajsr = F.jsr.r();
+  cass = F.ss.r();
   // ---- voltage terms at the substep start, one exponential per lane ----
   const R x = dep[0] + cA;
   R q = x * cR;
@@ -624,8 +656,8 @@ __device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStag
   for (int i = 0; i < 3; i++) dep[i] = L.dep0[i] + frac * L.span[i];
   ghk_terms(dep[0], pca_scale, e2, a2j, small);
   fcn_fru4(g, y1J, y1S, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
-  F.cajsr64 = F.cajsr64 + (double)((k1J + dt * dJ) / R(2));
-  F.cass64 = F.cass64 + (double)((k1S + dt * dS) / R(2));
+  F.jsr.add((k1J + dt * dJ) / R(2));
+  F.ss.add((k1S + dt * dS) / R(2));
   // ---- transitions of this cleft's 8 channels (:215-276) ----
   bool moved = false;
   if (leave_gt(bw[0], dt, R0[0])) {
@@ -674,8 +706,8 @@ __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live
   LaneStage<R> L;
   lane_stage(*sc.p, g, L);
   Fru4<R> F;
-  F.cajsr64 = cajsr64;
-  F.cass64 = cass64;
+  F.jsr.set(cajsr64);
+  F.ss.set(cass64);
   F.w = w;
   F.mti = mti;
   F.nsub = nsub;
@@ -700,8 +732,8 @@ __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live
     regen_step(sc, lane, g, go, F, S);
     if (go) substep_b(F, S, L, g, sc);
   }
-  cajsr64 = F.cajsr64;
-  cass64 = F.cass64;
+  cajsr64 = F.jsr.get();
+  cass64 = F.ss.get();
   w = F.w;
   mti = F.mti;
   nsub = F.nsub;
@@ -975,7 +1007,8 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
   sc.dirty = false;
   Fru4<R> F;
   F.t = 0.0;
-  F.cajsr64 = F.cass64 = 0.0;
+  F.jsr.set(0.0);
+  F.ss.set(0.0);
   F.w = 0u;
   F.nsub = 0u;
   F.mti = 0;
@@ -1007,23 +1040,23 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
     sc.my_hold_epoch = s.hold_epoch + ff;
     bool restore = false;
     if (p.flags & kFlagResume) {
-      F.cajsr64 = s.frus_s[ff];
-      F.cass64 = s.frus_s[(g.c + 1) * nf + ff];
+      F.jsr.set(s.frus_s[ff]);
+      F.ss.set(s.frus_s[(g.c + 1) * nf + ff]);
       F.w = s.chan_s[g.c * nf + ff];
       F.mti = s.mti_s[ff];
       restore = (*sc.my_hold_epoch == p.epoch);
     } else {
-      F.cajsr64 = s.frus[ff];
-      F.cass64 = s.frus[(g.c + 1) * nf + ff];
+      F.jsr.set(s.frus[ff]);
+      F.ss.set(s.frus[(g.c + 1) * nf + ff]);
       F.w = s.chan[g.c * nf + ff];
       F.mti = s.mti[ff];
     }
     if (p.flags & kFlagSave) {
       if (g.c == 0) {
-        s.frus_s[ff] = F.cajsr64;
+        s.frus_s[ff] = F.jsr.get();
         s.mti_s[ff] = F.mti;
       }
-      s.frus_s[(g.c + 1) * nf + ff] = F.cass64;
+      s.frus_s[(g.c + 1) * nf + ff] = F.ss.get();
       s.chan_s[g.c * nf + ff] = F.w;
     }
     copy_row16(sc.m, restore ? s.mt_hold + (size_t)ff * kMtStride : s.mt + (size_t)ff * kMtStride, g);
@@ -1034,7 +1067,7 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
   auto finish = [&]() {
     if (sc.dirty) copy_row16(s.mt + (size_t)f * kMtStride, sc.m, g);
     if (g.c == 0) {
-      s.frus[f] = F.cajsr64;
+      s.frus[f] = F.jsr.get();
       s.mti[f] = F.mti;
       if (s.trace_sub) s.trace_sub[f] = F.nsub;
       atomicAdd(&s.qctl[3], F.nsub);
@@ -1044,7 +1077,7 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
         heavy_next[atomicAdd(&s.qctl[1 + (L & 1u)], 1u)] = f;
       }
     }
-    s.frus[(g.c + 1) * nf + f] = F.cass64;
+    s.frus[(g.c + 1) * nf + f] = F.ss.get();
     s.chan[g.c * nf + f] = F.w;
   };
   {
