@@ -109,6 +109,7 @@ def bind(path):
         "gw_download_range": ([vp, C.c_int, C.c_int, _dp, _ip, _ip, _ip], C.c_int),
         "gw_set_precision": ([vp, C.c_int], C.c_int),
         "gw_set_pca_scale": ([vp, C.c_double], C.c_int),
+        "gw_set_sum_order": ([vp, C.c_int], C.c_int),
         "gw_settings_init": ([P(Settings)], None),
         "gw_rk54pd": ([vp, P(Settings), C.c_double, C.c_double, C.c_double, _dp, _dp, P(C.c_double)], C.c_int),
         "gw_lastcall": ([vp, P(Settings), C.c_double, _dp, _dp], C.c_int),
@@ -136,6 +137,7 @@ def bind(path):
         "gw_l2_flush": ([vp], C.c_int),
         "gw_probe_fp64_peak": ([P(C.c_double)], C.c_int),
         "gw_probe_fcn": ([P(C.c_double), P(C.c_double)], C.c_int),
+        "gw_probe_exp": ([_dp, _dp, _dp, C.c_int], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name, None)
@@ -203,6 +205,14 @@ class Cell:
 
     def set_stage_packing(self, warps):
         _check(self._L.gw_set_stage_packing(self._h, int(warps)), "gw_set_stage_packing", self._L)
+
+    def set_sum_order(self, order):
+        """"tree" (default: one fixed parallel order for every launch shape) or
+        "reference" (the serial reference's FRU-by-FRU order; a parity mode
+        for small cells)."""
+        if order not in ("tree", "reference"):
+            raise ValueError("sum order must be 'tree' or 'reference'")
+        _check(self._L.gw_set_sum_order(self._h, 1 if order == "reference" else 0), "gw_set_sum_order", self._L)
 
     def set_fru_lanes(self, lanes):
         _check(self._L.gw_set_fru_lanes(self._h, int(lanes)), "gw_set_fru_lanes", self._L)
@@ -321,6 +331,15 @@ class Cell:
                              _ptr(cu)), "gw_run", self._L)
         self.oldstep = os_.value
         return tt.value, st, ot, cu
+
+
+def exp_device_and_host(x, lib=None):
+    """(device exp, host libm exp) of the float64 array x."""
+    L = lib if lib is not None else load()
+    x = np.ascontiguousarray(x, np.float64)
+    yd, yh = np.zeros_like(x), np.zeros_like(x)
+    _check(L.gw_probe_exp(x, yd, yh, len(x)), "gw_probe_exp", L)
+    return yd, yh
 
 
 def fcn_cost_us(lib=None):

@@ -184,6 +184,14 @@ extern "C" int gw_set_pca_scale(gw_ctx* c, double scale) {
   return GW_OK;
 }
 
+extern "C" int gw_set_sum_order(gw_ctx* c, int order) {
+  if (!c || (order != GW_SUM_TREE && order != GW_SUM_REFERENCE))
+    return set_err(GW_EINVAL, "gw_set_sum_order: order must be GW_SUM_TREE or GW_SUM_REFERENCE");
+  if (c->batch) return set_err(GW_EINVAL, "gw_set_sum_order: the cell is in a batch");
+  c->sum_order = order;
+  return GW_OK;
+}
+
 extern "C" int gw_sync(gw_ctx* c) {
   if (!c) return set_err(GW_EINVAL, "gw_sync: null context");
   CK(cudaStreamSynchronize(c->stream));
@@ -357,6 +365,10 @@ static int run_stage(gw_ctx* c, double t0, double tf, const double dep0[3], cons
   if (c->profiling) CK(cudaEventRecord(c->pev[0], c->stream));
   CK(launch_stage_variant(c, p));
   c->launches++;
+  if (c->sum_order == GW_SUM_REFERENCE) {
+    CK(gw::launch_flux_seq(c->d, p, c->stream));
+    c->launches++;
+  }
   if (c->profiling) CK(cudaEventRecord(c->pev[1], c->stream));
   CK(cudaMemcpyAsync(c->h_out, c->d.out, 32 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -394,7 +406,10 @@ extern "C" int gw_avg_sums(gw_ctx* c, double num[11]) {
   if (!c || !num) return set_err(GW_EINVAL, "gw_avg_sums: null argument");
   int rc = flush_pending(c);
   if (rc) return rc;
-  CK(gw::launch_avg(c->d, c->stream));
+  if (c->sum_order == GW_SUM_REFERENCE)
+    CK(gw::launch_avg_seq(c->d, c->stream));
+  else
+    CK(gw::launch_avg(c->d, c->stream));
   c->launches++;
   CK(cudaMemcpyAsync(c->h_out + 16, c->d.out + 16, 11 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -546,6 +561,12 @@ extern "C" int gw_l2_flush(gw_ctx* c) {
 extern "C" int gw_probe_fcn(double* device_us, double* host_us) {
   if (!device_us || !host_us) return set_err(GW_EINVAL, "gw_probe_fcn: null argument");
   CK(gw::probe_fcn(device_us, host_us));
+  return GW_OK;
+}
+
+extern "C" int gw_probe_exp(const double* x, double* device_y, double* host_y, int n) {
+  if (!x || !device_y || !host_y || n <= 0) return set_err(GW_EINVAL, "gw_probe_exp: bad argument");
+  CK(gw::probe_exp(x, device_y, host_y, n));
   return GW_OK;
 }
 

@@ -225,6 +225,8 @@ extern "C" int gw_batch_add(gw_batch* b, gw_ctx* c) {
   if (!b || !c || c->batch) return gw_internal_error(GW_EINVAL, "gw_batch_add: bad cell or cell already batched");
   if (c->fru_lanes != 4 || c->precision != b->precision)
     return gw_internal_error(GW_EINVAL, "gw_batch_add: cell precision / kernel differs from the batch's");
+  if (c->sum_order != GW_SUM_TREE)
+    return gw_internal_error(GW_EINVAL, "gw_batch_add: reference-order sums are a single-cell mode");
   std::lock_guard<std::mutex> lk(b->mu);
   cudaStreamSynchronize(c->stream);  // the cell's own pending work lands first
   c->batch = b;

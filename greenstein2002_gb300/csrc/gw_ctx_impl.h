@@ -28,6 +28,7 @@ struct gw_ctx {
   uint32_t pack_launch = 0; // packed launches so far
   int precision = 0;        // 0: FP64, 1: mixed (FP32 rates and local ODE)
   double pca_scale = 1.0;   // LCC permeability scale of the cell
+  int sum_order = 0;        // GW_SUM_TREE or GW_SUM_REFERENCE
   gw_batch* batch = nullptr;  // set while the cell is a member of a batch
   int slot = -1;              // its index in the batch
   double batch_out[32];       // its outputs of the last batch round

@@ -358,9 +358,11 @@ extern "C" int gw_run_device(int n, gw_ctx** cells, const gw_settings* sets, dou
     return gw_internal_error(GW_EINVAL, "gw_run_device: bad argument");
   const int prec = cells[0]->precision;
   for (int i = 0; i < n; i++)
-    if (!cells[i] || cells[i]->precision != prec || cells[i]->fru_lanes != 4 || cells[i]->batch)
+    if (!cells[i] || cells[i]->precision != prec || cells[i]->fru_lanes != 4 || cells[i]->batch ||
+        cells[i]->sum_order != GW_SUM_TREE)
       return gw_internal_error(GW_EINVAL,
-                               "gw_run_device: cells must share one precision, use the 4-lane kernel and not be batched");
+                               "gw_run_device: cells must share one precision, use the 4-lane kernel and tree-order "
+                               "sums and not be batched");
   const int warps = cells[0]->stage_warps;
   std::vector<gw::DevState> hcells(n);
   std::vector<int> hblock0(n + 1);

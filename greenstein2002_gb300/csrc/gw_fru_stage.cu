@@ -187,6 +187,111 @@ __global__ void __launch_bounds__(kStageThreads) fru_avg_kernel(DevState s) {
     for (int k = 0; k < 11; k++) s.out[16 + k] = tot[k];
 }
 
+// Reference-order sums (the parity mode of gw_set_sum_order): the flux
+// numerators added one FRU and one cleft after another, as
+// calc_fru_flux_local.c:44-70 does, then the currents of
+// mpi_master.c:447-468.  A sequential FP64 sum has exactly one rounding
+// order, so each sum is one thread's dependent chain; the block stages the
+// stored FRU states in shared memory in coalesced chunks and three warps (on
+// three SM sub-partitions) run the three chains side by side: the CaSS sum,
+// the CaJSR sum, and the open-LCC CaSS sum with the two counts (integers,
+// exact).  About 4 dependent FP64 additions per FRU, so this mode is for
+// parity runs of small cells.  Runs after the stage launch and overwrites
+// out[0..8].
+constexpr int kSeqThreads = 128, kSeqChunk = 512;
+__global__ void __launch_bounds__(kSeqThreads) fru_flux_seq_kernel(DevState s, StageParams p) {
+  __shared__ double sf[5][kSeqChunk];
+  __shared__ uint32_t sw[kClefts][kSeqChunk];
+  __shared__ double res[5];
+  const size_t nf = (size_t)s.stride;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double acc = 0.0;  // warp 0: sum CaSS; warp 1: sum CaJSR; warp 2: sum CaSS of open LCCs
+  int oca = 0, ncl = 0;
+  for (int base = 0; base < s.nfru; base += kSeqChunk) {
+    const int cnt = min(kSeqChunk, s.nfru - base);
+    for (int i = threadIdx.x; i < 5 * cnt; i += kSeqThreads) sf[i / cnt][i % cnt] = s.frus[(i / cnt) * nf + base + i % cnt];
+    for (int i = threadIdx.x; i < kClefts * cnt; i += kSeqThreads)
+      sw[i / cnt][i % cnt] = s.chan[(i / cnt) * nf + base + i % cnt];
+    __syncthreads();
+    if (lane == 0 && warp == 0) {
+      for (int j = 0; j < cnt; j++)
+#pragma unroll
+        for (int c = 0; c < kClefts; c++) acc += sf[c + 1][j];
+    } else if (lane == 0 && warp == 1) {
+      for (int j = 0; j < cnt; j++) acc += sf[0][j];
+    } else if (lane == 0 && warp == 2) {
+      for (int j = 0; j < cnt; j++)
+#pragma unroll
+        for (int c = 0; c < kClefts; c++) {
+          const uint32_t w = sw[c][j];
+          if (lcc_open(w)) {
+            acc = acc + sf[c + 1][j];
+            oca++;
+          }
+          if (cl_of(w) == 2) ncl++;
+        }
+    }
+    __syncthreads();
+  }
+  if (lane == 0 && warp < 3) {
+    res[warp == 0 ? 0 : warp == 1 ? 1 : 2] = acc;
+    if (warp == 2) {
+      res[3] = (double)oca;
+      res[4] = (double)ncl;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double tot[5] = {res[0], res[1], res[2], res[3], res[4]};
+    double cur[4];
+    currents_from_sums(s.nfru, p.nfru_scale, p.depf, tot, cur);
+    cur[2] = cur[2] * p.pca_scale;
+#pragma unroll
+    for (int k = 0; k < 5; k++) s.out[k] = tot[k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) s.out[5 + k] = cur[k];
+  }
+}
+
+// The 11 output sums in the order of calc_fru_avg_local.c:50-91 (one thread,
+// the parity mode's counterpart of fru_avg_kernel).
+__global__ void __launch_bounds__(32) fru_avg_seq_kernel(DevState s) {
+  if (threadIdx.x != 0) return;
+  const size_t nf = (size_t)s.stride;
+  double v[11];
+#pragma unroll
+  for (int k = 0; k < 11; k++) v[k] = 0.0;
+  int ready = 0;
+  for (int f = 0; f < s.nfru; f++) {
+    const double jsr = s.frus[f];
+    v[1] = v[1] + jsr;
+    v[6] = v[6] + jsr * (1.0 + CSQNtot / (KmCSQN + jsr));
+#pragma unroll
+    for (int c = 0; c < kClefts; c++) {
+      const double ss = s.frus[(c + 1) * nf + f];
+      const uint32_t w = s.chan[c * nf + f];
+      v[0] = v[0] + ss;
+      v[5] = v[5] + ss * (1.0 + BSRtot / (KBSR + ss) + BSLtot / (KBSL + ss));
+      int no = 0;
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) {
+        const int r = ryr_of(w, i);
+        no += ryr_open(r);
+        ready += (r == 1 || r == 2);
+      }
+      v[2] = v[2] + JRyRmax * ((double)no) * (jsr - ss);
+      v[3] = v[3] + (double)no;
+      if (lcc_of(w) <= 6) v[7] = v[7] + 1.0;
+      if (vdi_of(w) == 2) v[8] = v[8] + 1.0;
+      if (lcc_open(w)) v[9] = v[9] + 1.0;
+      if (cl_of(w) == 2) v[10] = v[10] + 1.0;
+    }
+  }
+  v[4] = (double)ready;
+#pragma unroll
+  for (int k = 0; k < 11; k++) s.out[16 + k] = v[k];
+}
+
 // Knuth initialisation of every FRU's MT19937 state (mt19937_local.c:76-92),
 // seeded either by base + j or by the formula of initialize_ran.c:30-34.
 __global__ void fru_seed_kernel(DevState s, int scheme, uint32_t base) {
@@ -226,6 +331,14 @@ cudaError_t launch_stage(const DevState& s, const StageParams& p, cudaStream_t s
 }
 cudaError_t launch_avg(const DevState& s, cudaStream_t st) {
   fru_avg_kernel<<<s.nblocks, kStageThreads, 0, st>>>(s);
+  return cudaGetLastError();
+}
+cudaError_t launch_flux_seq(const DevState& s, const StageParams& p, cudaStream_t st) {
+  fru_flux_seq_kernel<<<1, kSeqThreads, 0, st>>>(s, p);
+  return cudaGetLastError();
+}
+cudaError_t launch_avg_seq(const DevState& s, cudaStream_t st) {
+  fru_avg_seq_kernel<<<1, 32, 0, st>>>(s);
   return cudaGetLastError();
 }
 cudaError_t launch_seed(const DevState& s, int scheme, uint32_t base, cudaStream_t st) {

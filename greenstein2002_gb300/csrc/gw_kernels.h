@@ -117,11 +117,17 @@ cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, int warp
 cudaError_t launch_stage4_packed(const DevState& s, const StageParams& p, int warps, cudaStream_t st);
 cudaError_t launch_stage_mixed_packed(const DevState& s, const StageParams& p, int warps, cudaStream_t st);
 cudaError_t launch_avg(const DevState& s, cudaStream_t st);
+// reference-order (sequential) flux and output sums of the stored FRU states,
+// one thread; the flux launch overwrites out[0..8], the average one out[16..26]
+cudaError_t launch_flux_seq(const DevState& s, const StageParams& p, cudaStream_t st);
+cudaError_t launch_avg_seq(const DevState& s, cudaStream_t st);
 // FP64 FMA throughput of the device (TFLOP/s, best of a few launches).
 cudaError_t probe_fp64(int sms, double* tflops);
 // Microseconds per evaluation of the 37-state global right-hand side on one
 // GPU thread and on the host.
 cudaError_t probe_fcn(double* device_us, double* host_us);
+// exp of n arguments on the device and with the host libm.
+cudaError_t probe_exp(const double* x, double* device_y, double* host_y, int n);
 cudaError_t launch_seed(const DevState& s, int scheme, uint32_t base, cudaStream_t st);
 
 }  // namespace gw

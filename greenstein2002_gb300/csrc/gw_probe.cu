@@ -110,4 +110,30 @@ cudaError_t probe_fcn(double* device_us, double* host_us) {
   return e;
 }
 
+// exp() as the FRU kernels evaluate it (CUDA's double exp), element-wise,
+// next to the host libm's: the FRU path's only transcendental (rates
+// fru_rates_local.c:131-132, :346-348; GHK fcn_fru.c:80; currents
+// mpi_master.c:406), so the only arithmetic the device cannot share with
+// the reference's host build bit for bit.
+__global__ void exp_map(const double* x, double* y, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = exp(x[i]);
+}
+
+cudaError_t probe_exp(const double* x, double* device_y, double* host_y, int n) {
+  double *dx = nullptr, *dy = nullptr;
+  cudaError_t e = cudaMalloc(&dx, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&dy, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    exp_map<<<(n + 255) / 256, 256>>>(dx, dy, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(device_y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  cudaFree(dy);
+  for (int i = 0; i < n; i++) host_y[i] = exp(x[i]);
+  return e;
+}
+
 }  // namespace gw

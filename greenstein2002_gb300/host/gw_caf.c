@@ -23,7 +23,10 @@
  * reference's arithmetic) or 1 (mixed: FP32 rates and local ODE),
  * fru_lanes = 4 or 1, stage_warps = 1/2/4/8 (warps per block) and
  * stage_packing = 0 or D (packed launches with 1/D as many warps as 8-FRU
- * groups); none of the shapes changes a result.
+ * groups); none of the shapes changes a result.  sum_order = 0 (one fixed
+ * parallel order of the cross-FRU sums) or 1 (the serial reference's order,
+ * a parity mode for small cells: with it the output files of an FP64 run
+ * equal the reference program's byte for byte).
  *
  * Exact checkpoints (exact_restart = 1): beside the reference's r_*.N.txt
  * files, whose %g values cannot restart a run exactly, every checkpoint also
@@ -51,7 +54,7 @@ typedef struct {
     gw_settings s;
     int nfru, ts_sec, ic_file_flag, Ndump, filenumber0, seed_scheme;
     int write_fru_props_flag, fru_start, fru_end, fru_props_compat, exact_restart;
-    int precision, fru_lanes, stage_warps, stage_packing;
+    int precision, fru_lanes, stage_warps, stage_packing, sum_order;
     unsigned long seed_base;
     char ic_dir[512], output_dir[512], restart_file[512];
     char ic_states[128], ic_FRU[128], ic_LCh[128], ic_RyR[128], ic_Ito2[128];
@@ -124,6 +127,7 @@ static int set_key(run_cfg *c, const char *k, const char *v)
     if (!strcmp(k, "fru_lanes")) { c->fru_lanes = atoi(v); return 0; }
     if (!strcmp(k, "stage_warps")) { c->stage_warps = atoi(v); return 0; }
     if (!strcmp(k, "stage_packing")) { c->stage_packing = atoi(v); return 0; }
+    if (!strcmp(k, "sum_order")) { c->sum_order = atoi(v); return 0; }
 #define STR(field, name) if (!strcmp(k, name)) { snprintf(c->field, sizeof c->field, "%s", v); return 0; }
     STR(ic_dir, "ic_dir") STR(output_dir, "output_dir") STR(ic_states, "ic_states_file") STR(ic_FRU, "ic_FRU_file")
     STR(ic_LCh, "ic_LCh_file") STR(ic_RyR, "ic_RyR_file") STR(ic_Ito2, "ic_Ito2_file")
@@ -611,6 +615,7 @@ int main(int argc, char **argv)
     gw_set_scale(ctx, 12500.0 / c.nfru);
     if (gw_set_precision(ctx, c.precision) || gw_set_fru_lanes(ctx, c.fru_lanes) ||
         gw_set_stage_warps(ctx, c.stage_warps) || gw_set_pca_scale(ctx, c.s.scale_PCa) ||
+        gw_set_sum_order(ctx, c.sum_order) ||
         gw_set_stage_packing(ctx, c.stage_packing > 0 ? ((c.nfru + 7) / 8 + c.stage_packing - 1) / c.stage_packing : 0)) {
         fprintf(stderr, "execution settings: %s\n", gw_last_error());
         return 1;

@@ -108,6 +108,19 @@ int gw_set_precision(gw_ctx *ctx, int precision);
  * parameters_fcn_fru.c:48), applied to the LCC flux of every cleft and to ICa. */
 int gw_set_pca_scale(gw_ctx *ctx, double scale);
 
+/* Order of the cross-FRU sums (flux numerators, output sums).
+ * GW_SUM_TREE (default): one fixed parallel tree, the same bits for every
+ * launch shape.  GW_SUM_REFERENCE: the serial reference's order, one FRU and
+ * one cleft after another (calc_fru_flux_local.c:44-70,
+ * calc_fru_avg_local.c:50-91), computed by one GPU thread after each stage --
+ * a parity mode for small cells, so that whole-cell trajectories can be
+ * compared with the reference program bit for bit.  Single cells and
+ * per-stream runs only (a lockstep batch or the device-resident integrator
+ * returns GW_EINVAL for such a cell). */
+#define GW_SUM_TREE 0
+#define GW_SUM_REFERENCE 1
+int gw_set_sum_order(gw_ctx *ctx, int order);
+
 /* FRU-substeps executed since creation (workload counter). */
 int gw_substeps(gw_ctx *ctx, unsigned long long *count);
 /* Wait for all work of the context. */
@@ -140,6 +153,10 @@ int gw_probe_fp64_peak(double *tflops);
  * GPU thread and on the host: what a device-resident integrator would pay
  * per stage on GB300's FP64 rate. */
 int gw_probe_fcn(double *device_us, double *host_us);
+/* exp() of n arguments as the device evaluates it and with the host libm:
+ * exp is the FRU path's only transcendental, and the two may round
+ * differently in the last place. */
+int gw_probe_exp(const double *x, double *device_y, double *host_y, int n);
 
 /* Allocation-free FRU stage (no counterpart in the reference).  For callers
  * that cannot allocate device memory while they run -- cudaMalloc

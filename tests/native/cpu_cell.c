@@ -139,3 +139,5 @@ int gw_set_stage_warps(gw_ctx *c, int warps) { (void)c; return warps >= 1 && war
 int gw_set_stage_packing(gw_ctx *c, int warps) { (void)c; return warps >= 0 ? GW_OK : GW_EINVAL; }
 int gw_set_precision(gw_ctx *c, int precision) { (void)c; return precision == 0 ? GW_OK : GW_EINVAL; }
 int gw_set_pca_scale(gw_ctx *c, double scale) { (void)c; return scale == 1.0 ? GW_OK : GW_EINVAL; }
+/* the oracle's sums are always in the reference's order */
+int gw_set_sum_order(gw_ctx *c, int order) { (void)c; return order == 0 || order == 1 ? GW_OK : GW_EINVAL; }

@@ -32,3 +32,4 @@ def test_first_beat_transition_sequences(gw, lanes):
     assert np.max(np.abs(states[:, 0] - g["states"][:, 0])) < 0.5
     cai = g["states"][:, 6]
     assert np.max(np.abs(states[:, 6] - cai)) < 0.01 * (cai.max() - cai.min())
+

@@ -35,3 +35,20 @@ def test_gpu_launch_shapes_same_files(gw, tmp_path):
     for name in ("warps4", "packed4"):
         for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
             assert filecmp.cmp(tmp_path / "fixed" / f, tmp_path / name / f, shallow=False), (name, f)
+
+
+@pytest.mark.parametrize("shape", [{}, {"stage_packing": 4}])
+def test_gpu_driver_files_equal_reference_program(gw, tmp_path, shape):
+    """In the reference's sum order (sum_order=1) the host driver on the GPU
+    library writes the reference program's own output files byte for byte
+    (tests/golden/drv250: 250 FRUs from rest, 1 Hz, FRU j seeded 5489 + j,
+    50 ms; made by tests/golden/make_driver_files.py)."""
+    import filecmp
+    import subprocess
+    from conftest import GOLDEN
+    exe = os.path.join(ROOT, "greenstein2002_gb300", "_build", "gw_caf")
+    args = dict({"NFRU_sim": 250, "time_end": 50.0, "ic_file_flag": 0, "seed_scheme": 0, "seed_base": 5489,
+                 "sum_order": 1}, **shape)
+    subprocess.run([exe] + ["%s=%s" % kv for kv in args.items()], cwd=tmp_path, check=True, capture_output=True)
+    for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
+        assert filecmp.cmp(os.path.join(GOLDEN, "drv250", f), tmp_path / f, shallow=False), f

@@ -5,7 +5,8 @@ Bar: bit-exact for every integer/index quantity (channel states, MT19937
 words and positions, open counts); FP64 Ca concentrations and flux sums
 within a relative 1e-12 (CUDA's exp() and the host libm's may differ in the
 last unit in the last place; flux sums are summed in a fixed tree order
-instead of the reference's sequential order)."""
+instead of the reference's sequential order, unless the cell is switched to
+the reference's order)."""
 import ctypes as C
 import zlib
 
@@ -166,6 +167,62 @@ def test_closed_loop_matches_reference_20ms(gw, lanes):
     fin = cell.download()
     assert np.mean(fin["mti"] == g["final_mti"]) >= 0.99
     assert np.mean(np.all(fin["ryr"].reshape(250, -1) == g["final_ryr"].reshape(250, -1), axis=1)) >= 0.99
+
+
+@pytest.mark.parametrize("shape", ["lanes1", "lanes4", "packed"])
+def test_closed_loop_reference_sum_order(gw, shape):
+    """With the reference's order of the cross-FRU sums (gw_set_sum_order) the
+    GPU run follows the reference program bit for bit until the first
+    last-place difference of CUDA's exp from the host libm's reaches the
+    global state: NFRU=250, rest, 1 Hz, seeds 5489+j.  The first 10 ms of
+    per-ms states, output sums and stored currents are the reference's bits
+    (with the tree order they differ from the first ms); over 20 ms the states
+    agree to 1e-9 and 99% of FRUs end in identical channel states and draw
+    counts."""
+    g = golden("closed250.npz")
+    cell = gw.Cell(250, fru_lanes=1 if shape == "lanes1" else 4)
+    if shape == "packed":
+        cell.set_stage_packing(8)
+    cell.set_sum_order("reference")
+    st = gw.settings()
+    state = cell.init_rest(st, scheme=gw.SEED_BASE, base=5489)
+    _, states, other, cur = cell.run(state, 0.0, 20, set_=st)
+    np.testing.assert_array_equal(states[:10], g["states"][:10])
+    np.testing.assert_array_equal(other[:10], g["other"][:10])
+    np.testing.assert_array_equal(cur[:10], g["currents"][:10, 1:])
+    np.testing.assert_allclose(states, g["states"], rtol=1e-9, atol=1e-15)
+    fin = cell.download()
+    assert np.mean(fin["mti"] == g["final_mti"]) >= 0.99
+    assert np.mean(np.all(fin["ryr"].reshape(250, -1) == g["final_ryr"].reshape(250, -1), axis=1)) >= 0.99
+
+
+def test_device_exp_within_one_ulp_of_libm(gw):
+    """exp is the FRU path's only transcendental.  CUDA's and the host libm's
+    agree to one unit in the last place on the arguments the path takes
+    (LCC and VDI rates, GHK factors over V in [-100, 60] mV) and differ in it
+    for a few percent of them: the residual between the GPU and the
+    reference program once the sums are in the reference's order."""
+    rng = np.random.default_rng(5)
+    v = rng.uniform(-100.0, 60.0, 100000)
+    x = np.concatenate([0.012 * (v - 35.0), -0.05 * (v - 35.0), (v + 12.5) / 5.0, (v + 30.0) / 12.0,
+                        v / 26.7, 2.0 * v / 26.7])
+    yd, yh = gw.exp_device_and_host(x)
+    ulps = np.abs(yd.view(np.int64) - yh.view(np.int64))
+    print("device exp vs host libm: %.2f%% of %d arguments differ, by at most %d ulp" %
+          (100.0 * np.mean(ulps > 0), len(x), int(ulps.max())))
+    assert ulps.max() <= 1
+
+
+def test_sum_order_is_a_single_cell_mode(gw):
+    cell = gw.Cell(64)
+    cell.set_sum_order("reference")
+    b = gw.Batch("fp64")
+    with pytest.raises(gw.GWError):
+        b.run([cell], [gw.settings()], np.zeros(1), np.zeros((1, 37)), np.full(1, 0.1), 1, lockstep=True)
+    b.close()
+    with pytest.raises(ValueError):
+        cell.set_sum_order("sequential")
+    cell.close()
 
 
 @pytest.mark.parametrize("lanes", LANES)

@@ -61,6 +61,19 @@ def test_outputs_match_reference_rest_start(tmp_path, have_ref):
         assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
 
 
+def test_outputs_match_committed_reference_files(tmp_path):
+    """The committed output files of the reference program (tests/golden/drv250,
+    made by tests/golden/make_driver_files.py) are what the host driver over
+    the oracle writes: pins the fixture the GPU host-driver test compares with."""
+    from conftest import GOLDEN
+    gw_dir = tmp_path / "gw"
+    gw_dir.mkdir()
+    subprocess.run([cpu_driver(), "NFRU_sim=250", "time_end=50", "ic_file_flag=0", "seed_scheme=0",
+                    "seed_base=5489", "sum_order=1"], cwd=gw_dir, check=True, capture_output=True)
+    for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
+        assert filecmp.cmp(os.path.join(GOLDEN, "drv250", f), gw_dir / f, shallow=False), f
+
+
 def test_outputs_match_reference_ic_files(tmp_path, have_ref):
     # the reference's default initial conditions: ic/stable files, its own
     # per-FRU seed formula, 1000 FRUs (1250-FRU files)
