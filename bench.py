@@ -661,27 +661,34 @@ def precision_ensemble(G, args, dist):
     seeds, ms = args.precision_ensemble
     t_ms = np.arange(1, ms + 1, dtype=float)
     res = {}
+    chunk = 16  # cells run at once: one host integrator thread per host core
     for prec in ("fp64", "mixed"):
-        cells, sets, states = [], [], []
-        for k in range(seeds):
-            c = G.Cell(NFRU, precision=prec)
-            if prec == "fp64":
-                c.set_stage_packing(((NFRU + 7) // 8 + 3) // 4)  # the FP64 ensemble's tuned shape
-            st = G.settings()
-            states.append(c.init_rest(st, scheme=G.SEED_BASE, base=SEED + 100000 * k))
-            cells.append(c)
-            sets.append(st)
-        states = np.ascontiguousarray(np.array(states))
-        runner = G.Batch(prec)
-        t0 = time.perf_counter()
-        st_tr, ot_tr = runner.run(cells, sets, np.zeros(seeds), states, np.full(seeds, 0.1), ms, traces=True,
-                                  lockstep=False)
-        wall = time.perf_counter() - t0
-        print("precision ensemble: %s, %d cells x %d ms in %.1f s" % (prec, seeds, ms, wall), file=sys.stderr,
-              flush=True)
-        for c in cells:
-            c.close()
-        runner.close()
+        st_parts, ot_parts, wall = [], [], 0.0
+        for k0 in range(0, seeds, chunk):
+            ks = range(k0, min(seeds, k0 + chunk))
+            cells, sets, states = [], [], []
+            for k in ks:
+                c = G.Cell(NFRU, precision=prec)
+                if prec == "fp64":
+                    c.set_stage_packing(((NFRU + 7) // 8 + 3) // 4)  # the FP64 ensemble's tuned shape
+                st = G.settings()
+                states.append(c.init_rest(st, scheme=G.SEED_BASE, base=SEED + 100000 * k))
+                cells.append(c)
+                sets.append(st)
+            states = np.ascontiguousarray(np.array(states))
+            runner = G.Batch(prec)
+            t0 = time.perf_counter()
+            st_tr, ot_tr = runner.run(cells, sets, np.zeros(len(ks)), states, np.full(len(ks), 0.1), ms,
+                                      traces=True, lockstep=False)
+            wall += time.perf_counter() - t0
+            print("precision ensemble: %s, seeds %d-%d x %d ms, %.1f s so far" % (prec, k0, ks[-1], ms, wall),
+                  file=sys.stderr, flush=True)
+            for c in cells:
+                c.close()
+            runner.close()
+            st_parts.append(st_tr)
+            ot_parts.append(ot_tr)
+        st_tr, ot_tr = np.concatenate(st_parts), np.concatenate(ot_parts)
         res[prec] = {"apd90": np.array([apd90(t_ms, v) for v in st_tr[:, :, 0]]), "peak_cai": st_tr[:, :, 6].max(1),
                      "jsr": ot_tr[:, :, 1].mean(0), "plcc": ot_tr[:, :, 7].mean(0), "pryr": ot_tr[:, :, 3].mean(0),
                      "wall_s": wall}
@@ -704,7 +711,11 @@ def precision_ensemble(G, args, dist):
                                         "max_lcc": float(np.max(f["plcc"])),
                                         "max_abs_diff_ryr": float(np.max(np.abs(m["pryr"] - f["pryr"]))),
                                         "max_ryr": float(np.max(f["pryr"]))},
-            "wall_s": {"fp64": f["wall_s"], "mixed": m["wall_s"]}}
+            "wall_s": {"fp64": f["wall_s"], "mixed": m["wall_s"]},
+            "per_seed": {"apd90_fp64_ms": [None if np.isnan(x) else float(x) for x in f["apd90"]],
+                         "apd90_mixed_ms": [None if np.isnan(x) else float(x) for x in m["apd90"]],
+                         "peak_cai_fp64_mM": [float(x) for x in f["peak_cai"]],
+                         "peak_cai_mixed_mM": [float(x) for x in m["peak_cai"]]}}
 
 
 def run_gpu(args, dist):

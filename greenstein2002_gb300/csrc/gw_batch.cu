@@ -18,6 +18,7 @@
 #include <condition_variable>
 #include <mutex>
 #include <new>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -311,6 +312,7 @@ extern "C" int gw_run_concurrent(int n, gw_ctx** cells, const gw_settings* sets,
   if (n <= 0 || !cells || !sets || !t || !states || !oldsteps)
     return gw_internal_error(GW_EINVAL, "gw_run_concurrent: bad argument");
   std::vector<int> rcs(n, 0);
+  std::vector<std::string> msgs(n);
   std::vector<std::thread> th;
   th.reserve(n);
   int dev = 0;
@@ -321,9 +323,14 @@ extern "C" int gw_run_concurrent(int n, gw_ctx** cells, const gw_settings* sets,
       rcs[i] = gw_run(cells[i], &sets[i], &t[i], states + (size_t)i * 37, &oldsteps[i], n_steps,
                       state_trace ? state_trace + (size_t)i * n_steps * 37 : nullptr,
                       other_trace ? other_trace + (size_t)i * n_steps * 12 : nullptr, nullptr);
+      if (rcs[i]) msgs[i] = gw_last_error();  // the message is per thread
     });
   for (auto& x : th) x.join();
   for (int i = 0; i < n; i++)
-    if (rcs[i]) return rcs[i];
+    if (rcs[i]) {
+      const std::string m = "gw_run_concurrent: cell " + std::to_string(i) + ": " + msgs[i];
+      gw_internal_error(rcs[i], m.c_str());
+      return rcs[i];
+    }
   return GW_OK;
 }

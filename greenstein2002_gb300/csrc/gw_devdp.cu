@@ -210,6 +210,16 @@ __device__ __noinline__ void dp_after(DpCell& c, const double J[4], const double
   }
   const gw_settings& P = c.set;
   bool finished_output = false;
+  if (tr < P.tolrk || step <= P.step_min) {
+    // an accepted state that is not finite would only be accepted again at
+    // the minimum step, forever: the cell stops with an error instead
+    bool finite = true;
+    for (int i = 0; i < GW_NSTATE; i++) finite = finite && isfinite(y5[i]);
+    if (!finite) {
+      c.err = 2;
+      return;
+    }
+  }
   if (tr < P.tolrk) {
     for (int i = 0; i < GW_NSTATE; i++) {
       if (fabs(y5[i]) < min_tolvalue) y5[i] = 0.0;
@@ -329,7 +339,7 @@ __global__ void __launch_bounds__(32) dp_step_kernel(DpArgs a) {
         const double* avg = (c.sp.flags & kFlagAvg) ? o + 16 : nullptr;
         const double J[4] = {o[5], o[6], o[7], o[8]};
         dp_after(c, J, avg);
-        if (c.done) atomicSub(a.running, 1u);
+        if (c.done || c.err) atomicSub(a.running, 1u);
       }
     }
   }
@@ -510,8 +520,9 @@ extern "C" int gw_run_device(int n, gw_ctx** cells, const gw_settings* sets, dou
     for (int i = 0; i < n; i++) {
       const DpCell& d = hdp[i];
       if (d.err || !d.done) {
-        rc = gw_internal_error(GW_EINVAL, d.err ? "gw_run_device: substep limit reached (corrupted FRU state)"
-                                                : "gw_run_device: a cell did not finish its output steps");
+        rc = gw_internal_error(GW_EINVAL, d.err == 1   ? "gw_run_device: substep limit reached (corrupted FRU state)"
+                                          : d.err == 2 ? "gw_run_device: global state not finite"
+                                                       : "gw_run_device: a cell did not finish its output steps");
         break;
       }
       memcpy(states + (size_t)i * GW_NSTATE, d.y, sizeof d.y);

@@ -13,6 +13,7 @@
  * the reference's to the last bit wherever libm agrees.
  */
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -24,6 +25,17 @@
 #define GW_MAX(a, b) ((a) < (b) ? (b) : (a))
 
 void gw_settings_init(gw_settings *s) { gw_protocol_defaults(s); }
+
+/* Error reporting of the library that links this file (gw_abi.cu, or a
+ * test stand-in). */
+int gw_internal_error(int code, const char *msg);
+
+static int gw_dp_error(double t, int i)
+{
+    char msg[96];
+    snprintf(msg, sizeof msg, "gw_rk54pd: global state %d not finite at t = %.9g ms", i, t);
+    return gw_internal_error(GW_EINVAL, msg);
+}
 
 static void dep_of(const double *y, double d[3])
 {
@@ -119,6 +131,12 @@ int gw_rk54pd(gw_ctx *ctx, const gw_settings *P, double t, double tstep, double 
             err = fabs((ym[i] - y1[i]) * 0.2 * gw_errweight(i));
             if (err < huge_number) tr = GW_MAX(err, tr);
             else tr = huge_number;
+        }
+        if (tr < P->tolrk || step <= P->step_min) {
+            /* a state that is not finite would only be accepted again at the
+             * minimum step, forever (the reference crawls on): stop instead */
+            for (i = 0; i < NS; i++)
+                if (!isfinite(y1[i])) return gw_dp_error(start, i);
         }
         if (tr < P->tolrk) {
             /* accept, rk_pd54m.c:241-286 */

@@ -67,6 +67,19 @@ __device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rexp(float x) { return expf(x); }
+// e = exp(x) and the GHK denominator e - 1.  FP64: the reference's e - 1.
+// FP32: expm1f, because expf(x) - 1 keeps almost no relative precision for
+// the |x| < 1e-5 of membrane potentials within a few tenths of a mV of zero,
+// and is exactly 0 for potentials of a few uV (just above the 1e-6 mV of the
+// reference's V = 0 branch), which made the GHK factor infinite.
+__device__ __forceinline__ void exp_em1(double x, double& e, double& em1) {
+  e = exp(x);
+  em1 = e - 1.0;
+}
+__device__ __forceinline__ void exp_em1(float x, float& e, float& em1) {
+  em1 = expm1f(x);
+  e = 1.0f + em1;
+}
 
 // FP64: u = y/2^32 compared with P = 1 - dt*R in the integer domain.
 __device__ __forceinline__ void thresh(double P, uint64_t& fl, bool& exact) {
@@ -352,10 +365,11 @@ __device__ __forceinline__ void ghk_terms(R V, R pca_scale, R& e2, R& a2j, bool&
   constexpr double JDHconstant = 1.0 / (2.0 * VSS * Faraday * 1000.0);
   const R VFRT = divc(V, R(RT_over_F), R(1.0 / RT_over_F));
   const R VFsqRT = R(1000.0 * Faraday) * VFRT;
-  e2 = rexp(R(2) * VFRT);
+  R em1;
+  exp_em1(R(2) * VFRT, e2, em1);
   small = abs_lt(V, R(1.e-6));
   if (small) a2j = R(0);
-  else a2j = rdiv(R(PCa * 4.0) * pca_scale * VFsqRT, e2 - R(1)) * R(JDHconstant);
+  else a2j = rdiv(R(PCa * 4.0) * pca_scale * VFsqRT, em1) * R(JDHconstant);
 }
 
 // (t - t0) / interval with r = 1/interval rounded once per stage: Markstein's

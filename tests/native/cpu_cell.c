@@ -6,6 +6,7 @@
  * compare them with the reference build.  Never part of the product.
  */
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -55,7 +56,13 @@ static void copy_set(set_t *d, const set_t *s, int n)
     if (d->mt) memcpy(d->mt, s->mt, sizeof(uint32_t) * 624 * n);
 }
 
-const char *gw_last_error(void) { return "cpu test stand-in"; }
+static char g_err[256] = "cpu test stand-in";
+const char *gw_last_error(void) { return g_err; }
+int gw_internal_error(int code, const char *msg)
+{
+    snprintf(g_err, sizeof g_err, "%s", msg);
+    return code;
+}
 int gw_create(gw_ctx **out, int n)
 {
     gw_ctx *c = calloc(1, sizeof *c);

@@ -77,3 +77,19 @@ def test_matches_host_integrator(gw, prec):
     assert dv < 0.05
     assert t[0] == steps
     np.testing.assert_allclose(ot_dev[0][:, 1], ot_host[:, 1], rtol=1e-3)
+
+
+def test_non_finite_state_stops_both_integrators(gw):
+    """A cell whose global state is not finite (NaN in the total-Ca
+    accumulator, state 31, which feeds no other derivative, so the FRU
+    launches see finite inputs) ends the run with an error, on the device
+    integrator and on the host one, instead of crawling at the minimum step."""
+    cells, sets, states = _cells(gw, [200, 300], "fp64")
+    states[1, 31] = np.nan
+    with pytest.raises(gw.GWError, match="not finite"):
+        gw.run_device(cells, sets, np.zeros(2), states, np.full(2, 0.1), 2)
+    cells, sets, states = _cells(gw, [200], "fp64")
+    state = np.ascontiguousarray(states[0])
+    state[31] = np.nan
+    with pytest.raises(gw.GWError, match="not finite"):
+        cells[0].run(state, 0.0, 1, set_=sets[0])

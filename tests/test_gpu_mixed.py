@@ -47,6 +47,25 @@ def test_mixed_stage_tracks_fp64(gw):
     assert rel.max() < 1e-4, rel.max()
 
 
+@pytest.mark.parametrize("v_uV", [1.5, 3.0, 30.0, -2.0])
+def test_mixed_ghk_near_zero_potential(gw, v_uV):
+    """The GHK factor of the LCC flux at membrane potentials of a few uV
+    (just above the reference's |V| < 1e-6 mV branch): the FP32 path keeps
+    e - 1 from expm1, so the FRU Ca states stay finite and track FP64."""
+    rng = np.random.default_rng(12)
+    n = 2000
+    s = _random_set(rng, n, 77)
+    v = v_uV * 1e-3
+    out = {}
+    for prec in ("fp64", "mixed"):
+        cell = gw.Cell(n, precision=prec)
+        cell.upload(s)
+        num = cell.stage(5.0, 5.05, [v, 2e-4, 0.7], [v, 2e-4, 0.7])[1]
+        out[prec] = (num, cell.download()["frus"])
+    assert np.all(np.isfinite(out["mixed"][1])) and np.all(np.isfinite(out["mixed"][0]))
+    np.testing.assert_allclose(out["mixed"][0][:3], out["fp64"][0][:3], rtol=1e-2)
+
+
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_total_calcium_is_conserved(gw, prec):
     cell = gw.Cell(250, precision=prec)

@@ -105,6 +105,19 @@ def test_closed_loop_host_driver_matches_reference(cpu_cell_lib):
     np.testing.assert_array_equal(fin["ryr"], g["final_ryr"])
 
 
+def test_integrator_stops_on_non_finite_state(cpu_cell_lib):
+    """A global state that is not finite stops the run with an error instead
+    of being force-accepted at the minimum step over and over (NaN in the
+    total-Ca accumulator, state 31, which feeds no other derivative)."""
+    import greenstein2002_gb300 as G
+    cell = G.Cell(32, lib=cpu_cell_lib)
+    st = G.settings()
+    state = cell.init_rest(st, scheme=G.SEED_BASE, base=5489)
+    state[31] = np.nan
+    with pytest.raises(G.GWError, match="not finite"):
+        cell.run(state, 0.0, 1, set_=st)
+
+
 @pytest.fixture(scope="module")
 def ref():
     r = O.ref_lib()
