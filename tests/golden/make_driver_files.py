@@ -1,9 +1,13 @@
 """Golden output files of the reference program for the GPU host-driver test.
 
-Builds the reference serially (oracle/build_ref.py) for 250 FRUs, the rest
-initial state (ic_file_flag 0), the 1 Hz stimulus and 50 ms, runs it with FRU
-j seeded 5489 + j, and copies the files it writes (states.0.txt,
-otherstates.0.txt, currents.0.txt; data_io.c:22-140) to tests/golden/drv250/.
+Builds the reference serially (oracle/build_ref.py) for 250 FRUs and the rest
+initial state (ic_file_flag 0), runs it with FRU j seeded 5489 + j, and copies
+the files it writes (states.0.txt, otherstates.0.txt, currents.0.txt;
+data_io.c:22-140):
+  tests/golden/drv250/          the 1 Hz stimulus, 50 ms
+  tests/golden/drv250_vclamp/   the voltage clamp of fcn.c:448-480 (hold
+                                -100 mV, 0 mV for 200 ms from 10 ms, period
+                                500 ms), 30 ms
 Runs only where the reference sources are available; the files are committed.
 
 Usage: python tests/golden/make_driver_files.py
@@ -18,21 +22,24 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import build_ref  # noqa: E402
 
-NFRU, TIME_END, SEED_BASE = 250, 50.0, 5489
+NFRU, SEED_BASE = 250, 5489
 FILES = ("states.0.txt", "otherstates.0.txt", "currents.0.txt")
+VCLAMP = {"hold": -100.0, "set": 0.0, "duration": 200.0, "shift": 10.0, "period": 500.0}
+CASES = {"drv250": (50.0, None), "drv250_vclamp": (30.0, VCLAMP)}
 
 
 def main():
     if not build_ref.have_sources():
         sys.exit("reference sources not available")
-    d = build_ref.build_config("drv_%d_%d_0" % (NFRU, int(TIME_END)), build_ref.cfg_macros(NFRU, TIME_END))
-    out = os.path.join(HERE, "drv%d" % NFRU)
-    os.makedirs(out, exist_ok=True)
-    with tempfile.TemporaryDirectory() as work:
-        build_ref.run_stoch(d, work, seed_base=SEED_BASE)
-        for f in FILES:
-            shutil.copyfile(os.path.join(work, f), os.path.join(out, f))
-    print("wrote", out)
+    for name, (time_end, vclamp) in CASES.items():
+        d = build_ref.build_config("gold_" + name, build_ref.cfg_macros(NFRU, time_end, vclamp=vclamp))
+        out = os.path.join(HERE, name)
+        os.makedirs(out, exist_ok=True)
+        with tempfile.TemporaryDirectory() as work:
+            build_ref.run_stoch(d, work, seed_base=SEED_BASE)
+            for f in FILES:
+                shutil.copyfile(os.path.join(work, f), os.path.join(out, f))
+        print("wrote", out)
 
 
 if __name__ == "__main__":

@@ -6,7 +6,7 @@ import os
 import pytest
 
 from conftest import ROOT
-from test_host_driver import exact_restart_case
+from test_host_driver import GOLDEN_DRIVER_CASES, exact_restart_case, golden_driver_args
 
 pytestmark = pytest.mark.gpu
 
@@ -38,17 +38,18 @@ def test_gpu_launch_shapes_same_files(gw, tmp_path):
 
 
 @pytest.mark.parametrize("shape", [{}, {"stage_packing": 4}])
-def test_gpu_driver_files_equal_reference_program(gw, tmp_path, shape):
+@pytest.mark.parametrize("case", sorted(GOLDEN_DRIVER_CASES))
+def test_gpu_driver_files_equal_reference_program(gw, tmp_path, case, shape):
     """In the reference's sum order (sum_order=1) the host driver on the GPU
-    library writes the reference program's own output files byte for byte
-    (tests/golden/drv250: 250 FRUs from rest, 1 Hz, FRU j seeded 5489 + j,
-    50 ms; made by tests/golden/make_driver_files.py)."""
+    library writes the reference program's own output files byte for byte:
+    250 FRUs from rest, FRU j seeded 5489 + j, 50 ms of 1 Hz pacing or 30 ms
+    through a voltage-clamp step (tests/golden/drv250*, made by
+    tests/golden/make_driver_files.py)."""
     import filecmp
     import subprocess
     from conftest import GOLDEN
     exe = os.path.join(ROOT, "greenstein2002_gb300", "_build", "gw_caf")
-    args = dict({"NFRU_sim": 250, "time_end": 50.0, "ic_file_flag": 0, "seed_scheme": 0, "seed_base": 5489,
-                 "sum_order": 1}, **shape)
+    args = dict(golden_driver_args(case), **shape)
     subprocess.run([exe] + ["%s=%s" % kv for kv in args.items()], cwd=tmp_path, check=True, capture_output=True)
     for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
-        assert filecmp.cmp(os.path.join(GOLDEN, "drv250", f), tmp_path / f, shallow=False), f
+        assert filecmp.cmp(os.path.join(GOLDEN, case, f), tmp_path / f, shallow=False), f

@@ -61,17 +61,31 @@ def test_outputs_match_reference_rest_start(tmp_path, have_ref):
         assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
 
 
-def test_outputs_match_committed_reference_files(tmp_path):
-    """The committed output files of the reference program (tests/golden/drv250,
+GOLDEN_DRIVER_CASES = {
+    # tests/golden/<name>: the reference program's files (tests/golden/make_driver_files.py)
+    "drv250": {"time_end": 50.0},
+    "drv250_vclamp": {"time_end": 30.0, "vclamp_flag": 1, "vclamp_hold": -100.0, "vclamp_set": 0.0,
+                      "vclamp_duration": 200.0, "vclamp_shift": 10.0, "vclamp_period": 500.0},
+}
+
+
+def golden_driver_args(name):
+    return dict({"NFRU_sim": 250, "ic_file_flag": 0, "seed_scheme": 0, "seed_base": 5489, "sum_order": 1},
+                **GOLDEN_DRIVER_CASES[name])
+
+
+@pytest.mark.parametrize("case", sorted(GOLDEN_DRIVER_CASES))
+def test_outputs_match_committed_reference_files(tmp_path, case):
+    """The committed output files of the reference program (tests/golden/drv250*,
     made by tests/golden/make_driver_files.py) are what the host driver over
-    the oracle writes: pins the fixture the GPU host-driver test compares with."""
+    the oracle writes: pins the fixtures the GPU host-driver test compares with."""
     from conftest import GOLDEN
     gw_dir = tmp_path / "gw"
     gw_dir.mkdir()
-    subprocess.run([cpu_driver(), "NFRU_sim=250", "time_end=50", "ic_file_flag=0", "seed_scheme=0",
-                    "seed_base=5489", "sum_order=1"], cwd=gw_dir, check=True, capture_output=True)
+    subprocess.run([cpu_driver()] + ["%s=%s" % kv for kv in golden_driver_args(case).items()], cwd=gw_dir,
+                   check=True, capture_output=True)
     for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
-        assert filecmp.cmp(os.path.join(GOLDEN, "drv250", f), gw_dir / f, shallow=False), f
+        assert filecmp.cmp(os.path.join(GOLDEN, case, f), gw_dir / f, shallow=False), f
 
 
 def test_outputs_match_reference_ic_files(tmp_path, have_ref):
@@ -81,6 +95,20 @@ def test_outputs_match_reference_ic_files(tmp_path, have_ref):
     ic = os.path.join(build_ref.SRC, "ic", "stable")
     ref_dir, gw_dir = _run_both(tmp_path, m, {"NFRU_sim": 1000, "time_end": 12.0, "ic_file_flag": 1,
                                               "ic_dir": ic, "seed_scheme": 1}, None)
+    for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
+        assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
+
+
+def test_outputs_match_reference_voltage_clamp(tmp_path, have_ref):
+    """The voltage-clamp protocol (fcn.c:448-480; hold -100 mV, step to 0 mV
+    for 200 ms from 10 ms, period 500 ms): the host driver's files equal the
+    reference program's byte for byte through the step."""
+    vc = {"hold": -100.0, "set": 0.0, "duration": 200.0, "shift": 10.0, "period": 500.0}
+    m = build_ref.cfg_macros(250, 30.0, vclamp=vc)
+    ref_dir, gw_dir = _run_both(tmp_path, m, {"NFRU_sim": 250, "time_end": 30.0, "ic_file_flag": 0,
+                                              "seed_scheme": 0, "seed_base": 5489, "vclamp_flag": 1,
+                                              "vclamp_hold": -100.0, "vclamp_set": 0.0, "vclamp_duration": 200.0,
+                                              "vclamp_shift": 10.0, "vclamp_period": 500.0}, 5489)
     for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
         assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
 
