@@ -57,7 +57,7 @@ class Request(C.Structure):
     _fields_ = [("nfru", C.c_int), ("set", Settings), ("seed_scheme", C.c_int), ("seed", C.c_uint32),
                 ("pca_scale", C.c_double), ("duration_ms", C.c_double), ("v_trace", C.c_void_p),
                 ("final_state", C.c_void_p), ("t_submit", C.c_double), ("t_start", C.c_double),
-                ("t_done", C.c_double), ("status", C.c_int)]
+                ("t_done", C.c_double), ("status", C.c_int), ("message", C.c_char * 160)]
 
 
 _lib = None

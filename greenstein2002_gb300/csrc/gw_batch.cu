@@ -285,6 +285,7 @@ extern "C" int gw_batch_run(gw_batch* b, int n, gw_ctx** cells, const gw_setting
     }
   }
   std::vector<int> rcs(n, 0);
+  std::vector<std::string> msgs(n);
   std::vector<std::thread> th;
   th.reserve(n);
   int dev = 0;
@@ -295,11 +296,16 @@ extern "C" int gw_batch_run(gw_batch* b, int n, gw_ctx** cells, const gw_setting
       rcs[i] = gw_run(cells[i], &sets[i], &t[i], states + (size_t)i * 37, &oldsteps[i], n_steps,
                       state_trace ? state_trace + (size_t)i * n_steps * 37 : nullptr,
                       other_trace ? other_trace + (size_t)i * n_steps * 12 : nullptr, nullptr);
+      if (rcs[i]) msgs[i] = gw_last_error();  // the message is per thread
       gw_batch_remove(b, cells[i]);
     });
   for (auto& x : th) x.join();
   for (int i = 0; i < n; i++)
-    if (rcs[i]) return rcs[i];
+    if (rcs[i]) {
+      const std::string m = "gw_batch_run: cell " + std::to_string(i) + ": " + msgs[i];
+      gw_internal_error(rcs[i], m.c_str());
+      return rcs[i];
+    }
   return GW_OK;
 }
 

@@ -12,6 +12,7 @@
 // seen.  Each request starts from the rest state with its own seeds, so its
 // result is the same alone and in any mix.
 #include <cuda_runtime.h>
+#include <stdio.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -101,6 +102,7 @@ static void run_request(gw_server* s, gw_request* r) {
     s->pool[r->nfru].push_back(c);
   }
   r->t_done = now_s();
+  if (rc) snprintf(r->message, sizeof r->message, "%s", gw_last_error());  // per-thread message
   r->status = rc;
 }
 

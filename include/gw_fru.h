@@ -291,6 +291,7 @@ typedef struct gw_request {
   double *final_state;     /* optional host buffer [37] */
   double t_submit, t_start, t_done; /* host clock seconds, set by the server */
   int status;              /* -1 while pending, then a GW_* status */
+  char message[160];       /* the error message when status is not GW_OK */
 } gw_request;
 typedef struct gw_server gw_server;
 /* Device bytes a cell of nfru FRUs holds (the admission unit). */

@@ -78,3 +78,19 @@ def test_no_device_is_an_error_not_a_fallback(lib):
     assert rc != 0
     with pytest.raises(G.GWError):
         G.Cell(16)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of gw_settings and gw_request have the C layout."""
+    import greenstein2002_gb300 as G
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "gw_fru.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(gw_settings), sizeof(gw_request),'
+                   ' offsetof(gw_request, set), offsetof(gw_request, duration_ms), offsetof(gw_request, status),'
+                   ' offsetof(gw_request, message)); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.check_call([os.environ.get("CC", "gcc"), "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(x) for x in subprocess.check_output([str(exe)], text=True).split()]
+    R = G.Request
+    assert got == [C.sizeof(G.Settings), C.sizeof(R), R.set.offset, R.duration_ms.offset, R.status.offset,
+                   R.message.offset]

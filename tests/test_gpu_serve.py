@@ -66,3 +66,18 @@ def test_admission_by_device_bytes(gw):
         live += d
         peak = max(peak, live)
     assert peak <= 2
+
+
+def test_failed_request_carries_its_message(gw):
+    """A request that fails (here: an unknown seeding scheme, refused on the
+    host before any launch) reports its status and message; the requests
+    beside it run normally."""
+    srv = gw.Server("mixed", slots=2, mem_budget_bytes=1 << 30)
+    bad, good = _req(gw, 200, 1, dur=2), _req(gw, 200, 2, dur=2)
+    bad.seed_scheme = 7
+    srv.submit(bad)
+    srv.submit(good)
+    srv.wait()
+    srv.close()
+    assert bad.status != 0 and b"scheme 7" in bad.message
+    assert good.status == 0 and good.message == b""
