@@ -3,6 +3,7 @@ aggregate whole-job throughput as the sum of the ranks' work over the
 slowest rank's time, and the reference arm runs on rank 0 only."""
 import json
 import os
+import re
 import socket
 import subprocess
 import sys
@@ -42,7 +43,8 @@ def test_dist_sum_and_max(tmp_path):
     script.write_text(HELPER % ROOT)
     r = _torchrun([str(script)])
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = sorted(l for l in r.stdout.splitlines() if l.startswith("RANK"))
+    # the ranks share one stdout, so their lines may interleave
+    lines = sorted(re.findall(r"RANK\d \S+ \S+?(?=RANK|\s|$)", r.stdout))
     assert lines == ["RANK0 3 10", "RANK1 3 10"]
 
 
