@@ -6,9 +6,11 @@ pacing with a 1 ms -100 uA/uF stimulus at 10 ms, 64 seeds for ensemble
 statistics): `value` is the throughput of an ensemble of --seeds cells (cell
 k's FRU j seeded 5489 + 100000 k + j) running on the GPU at once, one stream
 and one host integrator thread per cell -- the same kind of throughput the
-reference arm measures with one cell per host core.  Four cells already keep
-the FP64 pipe saturated (1, 4, 16 and 64 cells gave 8.5, 14.4, 14.4 and 14.4
-cell-ms/s over [30, 40) ms).  A step advances every cell by STEP_MS (10 ms) of
+reference arm measures with one cell per host core, and the same number of
+cells (16) as that arm runs on the host's 16 cores.  With packed launches
+(16-64 FRUs per warp, each cell a few hundred warps) more cells fill more of
+the FP64 pipe: 4, 8 and 16 cells gave 51.4, 51.7 and 70.4 cell-ms/s (the 8-cell
+figure over the heavier [30, 130) ms).  A step advances every cell by STEP_MS (10 ms) of
 simulated time through the whole hot path (Dormand-Prince global step, every
 FRU stage on the GPU).  Warm-up steps cover [0, W*10) ms (the stimulus and
 upstroke), so with the defaults (W=3, K=20) the timed window is [30, 230) ms:
@@ -71,7 +73,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gw", choices=["gw", "reference"])
     ap.add_argument("--nfru", type=int, default=NFRU)
-    ap.add_argument("--seeds", type=int, default=4,
+    ap.add_argument("--seeds", type=int, default=16,
                     help="cells of the FP64 ensemble (seeds k: FRU j seeded 5489 + 100000 k + j) run at once")
     ap.add_argument("--step-ms", type=float, default=STEP_MS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
