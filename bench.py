@@ -64,6 +64,24 @@ SEED = 5489
 TRAFFIC_PER_LAUNCH_12500 = 5 * 6.672128e6
 FLOPS_PER_SUBSTEP = 700.0
 BYTES_PER_SUBSTEP = 384.0
+# GB300 FP32 (non-tensor) peak, nominal: 152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
+def mixed_roofline(substeps_per_s, hbm_peak_gbs):
+    """The two candidate bounds of the mixed-precision path: its FP32 work
+    (700 FLOP per FRU-substep against the nominal FP32 peak) and its bytes
+    (384 B per FRU-substep against the measured copy bandwidth).  The larger
+    fraction is the binding one."""
+    tf = FLOPS_PER_SUBSTEP * substeps_per_s / 1e12
+    gbs = BYTES_PER_SUBSTEP * substeps_per_s / 1e9
+    f32 = {"achieved": tf, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s", "frac": tf / FP32_NOMINAL_TFLOPS,
+           "peak_source": "nominal (152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz)"}
+    hbm = {"achieved": gbs, "peak": hbm_peak_gbs, "unit": "GB/s", "frac": gbs / hbm_peak_gbs,
+           "peak_source": "measured copy bandwidth"}
+    return {"fp32": f32, "hbm": hbm, "binding": "fp32" if f32["frac"] >= hbm["frac"] else "hbm",
+            "algorithmic": "700 FLOP and 384 B per FRU-substep"}
+
 
 
 def parse():
@@ -756,8 +774,9 @@ def run_gpu(args, dist):
         m = time_single(G, args, dist, "mixed", seed, keep_trace=True)
         a, b = one["trace"], m["trace"]
         cai_range = float(np.max(a[:, 6]) - np.min(a[:, 6])) or 1.0
+        m_rate = m["substeps"] / (m["wall_ms"] / 1000.0)
         mixed = {"value": m["value"], "unit": "cell-ms/s (one cell)", "speedup_vs_fp64_one_cell": m["value"] / one["value"],
-                 "fru_substeps_per_s": m["substeps"] / (m["wall_ms"] / 1000.0), "tuning": m["tuning"],
+                 "fru_substeps_per_s": m_rate, "tuning": m["tuning"], "roofline": mixed_roofline(m_rate, hbm_peak),
                  "error_vs_fp64_same_seeds": {
                      "max_abs_dV_mV": float(np.max(np.abs(a[:, 0] - b[:, 0]))),
                      "max_abs_dCai_rel_to_range": float(np.max(np.abs(a[:, 6] - b[:, 6]))) / cai_range,
