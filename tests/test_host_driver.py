@@ -11,6 +11,7 @@ import os
 import subprocess
 import sys
 
+import numpy as np
 import pytest
 
 from conftest import ROOT, TBUILD, cpu_cell_lib_path
@@ -109,6 +110,39 @@ def test_outputs_match_reference_voltage_clamp(tmp_path, have_ref):
                                               "seed_scheme": 0, "seed_base": 5489, "vclamp_flag": 1,
                                               "vclamp_hold": -100.0, "vclamp_set": 0.0, "vclamp_duration": 200.0,
                                               "vclamp_shift": 10.0, "vclamp_period": 500.0}, 5489)
+    for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
+        assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
+
+
+PROTOCOLS = {
+    # I-V protocol (fcn.c:521-533, caf.c:232-235): from -100 mV, 5-ms steps to -40, -30, -20 mV,
+    # one per 10-ms period
+    "iv": {"iv_flag": 1, "iv_clamp_duration": 5.0, "iv_clamp_period": 10.0, "iv_shift": 2.0,
+           "iv_clamp_set": -40.0, "iv_clamp_hold": -100.0, "iv_clamp_step": 10.0},
+    # paired-pulse clamp (fcn.c:485-515): -80 mV, 5 ms at -40 mV from 5 ms, then 10 ms at 0 mV
+    "vpp": {"vppclamp_flag": 1, "vppclamp_ppset": -40.0, "vppclamp_ppduration": 5.0, "vppclamp_shift": 5.0,
+            "vppclamp_set": 0.0, "vppclamp_duration": 10.0, "vppclamp_hold": -80.0, "vppclamp_period": 500.0},
+}
+
+
+@pytest.mark.parametrize("proto", sorted(PROTOCOLS))
+def test_outputs_match_reference_clamp_protocols(tmp_path, have_ref, proto):
+    """The I-V and paired-pulse clamp protocols: the host driver's files equal
+    the reference program's byte for byte (250 FRUs from rest, 30 ms)."""
+    extra = PROTOCOLS[proto]
+    m = build_ref.cfg_macros(250, 30.0)
+    m.update({k: repr(float(v)) if isinstance(v, float) else v for k, v in extra.items()})
+    d = build_ref.build_config("drv_250_30_%s" % proto, m)
+    ref_dir = tmp_path / "ref"
+    build_ref.run_stoch(d, str(ref_dir), seed_base=5489)
+    gw_dir = tmp_path / "gw"
+    gw_dir.mkdir()
+    settings = dict({"NFRU_sim": 250, "time_end": 30.0, "ic_file_flag": 0, "seed_scheme": 0, "seed_base": 5489},
+                    **extra)
+    subprocess.run([cpu_driver()] + ["%s=%s" % kv for kv in settings.items()], cwd=gw_dir, check=True,
+                   capture_output=True)
+    v = np.loadtxt(ref_dir / "states.0.txt", skiprows=1)[:, 1]
+    assert len(set(np.round(v, 6))) >= 3  # the protocol moved V through its levels
     for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
         assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
 
