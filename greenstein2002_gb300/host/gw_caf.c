@@ -54,7 +54,7 @@ typedef struct {
     gw_settings s;
     int nfru, ts_sec, ic_file_flag, Ndump, filenumber0, seed_scheme;
     int write_fru_props_flag, fru_start, fru_end, fru_props_compat, exact_restart;
-    int precision, fru_lanes, stage_warps, stage_packing, sum_order;
+    int precision, fru_lanes, stage_warps, stage_packing, sum_order, reset_RyRs_flag;
     unsigned long seed_base;
     char ic_dir[512], output_dir[512], restart_file[512];
     char ic_states[128], ic_FRU[128], ic_LCh[128], ic_RyR[128], ic_Ito2[128];
@@ -114,6 +114,7 @@ static int set_key(run_cfg *c, const char *k, const char *v)
     if (!strcmp(k, "NFRU_sim") || !strcmp(k, "NFRU_sim_high") || !strcmp(k, "NFRU")) { c->nfru = atoi(v); return 0; }
     if (!strcmp(k, "ts_sec")) { c->ts_sec = atoi(v); return 0; }
     if (!strcmp(k, "ic_file_flag")) { c->ic_file_flag = atoi(v); return 0; }
+    if (!strcmp(k, "reset_RyRs_flag")) { c->reset_RyRs_flag = atoi(v); return 0; }
     if (!strcmp(k, "Ndump")) { c->Ndump = atoi(v); return 0; }
     if (!strcmp(k, "filenumber0")) { c->filenumber0 = atoi(v); return 0; }
     if (!strcmp(k, "seed_scheme")) { c->seed_scheme = atoi(v); return 0; }
@@ -557,9 +558,16 @@ static void init_cell(const run_cfg *c, gw_ctx *ctx, double *state)
     {
         double *frus = malloc(sizeof(double) * 5 * n), a1 = 0.0, a2 = 0.0;
         int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n);
-        int *ito2 = malloc(sizeof(int) * 4 * n), *mti = malloc(sizeof(int) * n), j, q;
+        int *ito2 = malloc(sizeof(int) * 4 * n), *mti = malloc(sizeof(int) * n), j, q, k;
         uint32_t *mt = calloc((size_t)624 * n, sizeof(uint32_t));
         read_ic(c, state, frus, ltype, ryr, ito2);
+        if (c->reset_RyRs_flag)  /* initialize_state.c:252-263: every LCC closed and available, every RyR in 1 */
+            for (j = 0; j < n; j++)
+                for (q = 0; q < 4; q++) {
+                    ltype[8 * j + 2 * q] = 1;
+                    ltype[8 * j + 2 * q + 1] = 2;
+                    for (k = 0; k < 5; k++) ryr[20 * j + 5 * q + k] = 1;
+                }
         for (j = 0; j < n; j++) mti[j] = 624;
         if (gw_upload(ctx, frus, ltype, ryr, ito2, mti, mt) || gw_seed(ctx, c->seed_scheme, (uint32_t)c->seed_base)) {
             fprintf(stderr, "initial upload failed: %s\n", gw_last_error());

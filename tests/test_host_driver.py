@@ -147,6 +147,29 @@ def test_outputs_match_reference_clamp_protocols(tmp_path, have_ref, proto):
         assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
 
 
+@pytest.mark.parametrize("variant", ["reset_RyRs", "chf"])
+def test_outputs_match_reference_ic_variants(tmp_path, have_ref, variant):
+    """From the reference's ic/stable files (250 FRUs, its seed formula, 8 ms):
+    reset_RyRs_flag (initialize_state.c:252-263: every LCC closed and
+    available, every RyR in state 1) and the heart-failure scalings of
+    chf_flag (fcn.c:780-785): the host driver's files equal the reference
+    program's byte for byte."""
+    extra = {"reset_RyRs": {"reset_RyRs_flag": 1}, "chf": {"chf_flag": 1}}[variant]
+    m = build_ref.cfg_macros(250, 8.0, ic_file=True)
+    m.update(extra)
+    d = build_ref.build_config("drv_250_8_ic_%s" % variant, m)
+    ref_dir = tmp_path / "ref"
+    build_ref.run_stoch(d, str(ref_dir))
+    gw_dir = tmp_path / "gw"
+    gw_dir.mkdir()
+    settings = dict({"NFRU_sim": 250, "time_end": 8.0, "ic_file_flag": 1,
+                     "ic_dir": os.path.join(build_ref.SRC, "ic", "stable"), "seed_scheme": 1}, **extra)
+    subprocess.run([cpu_driver()] + ["%s=%s" % kv for kv in settings.items()], cwd=gw_dir, check=True,
+                   capture_output=True)
+    for f in ("states.0.txt", "otherstates.0.txt", "currents.0.txt"):
+        assert filecmp.cmp(ref_dir / f, gw_dir / f, shallow=False), f
+
+
 def test_checkpoint_files(tmp_path, have_ref):
     """r_*.N.txt checkpoints every Ndump steps (data_io.c:197-268).  The
     reference's restart_data closes the r_states file twice (data_io.c:220
