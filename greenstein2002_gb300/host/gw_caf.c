@@ -50,6 +50,28 @@
 #include "gw_cell_model.h"
 #include "gw_fru.h"
 
+/* Host allocations: a run that cannot allocate stops with a message (the
+ * reference aborts on its fatal errors too). */
+static void *xmalloc(size_t bytes)
+{
+    void *p = malloc(bytes ? bytes : 1);
+    if (!p) {
+        fprintf(stderr, "gw_caf: out of host memory (%zu bytes)\n", bytes);
+        exit(6);
+    }
+    return p;
+}
+
+static void *xcalloc(size_t n, size_t size)
+{
+    void *p = calloc(n ? n : 1, size ? size : 1);
+    if (!p) {
+        fprintf(stderr, "gw_caf: out of host memory (%zu x %zu bytes)\n", n, size);
+        exit(6);
+    }
+    return p;
+}
+
 typedef struct {
     gw_settings s;
     int nfru, ts_sec, ic_file_flag, Ndump, filenumber0, seed_scheme;
@@ -295,8 +317,8 @@ static void write_row(FILE *f, const run_cfg *c, double t, const double *v, int 
 static void restart_data(const run_cfg *c, int num, const double *state, gw_ctx *ctx)
 {
     const int n = c->nfru;
-    double *frus = malloc(sizeof(double) * 5 * n);
-    int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n), *ito2 = malloc(sizeof(int) * 4 * n);
+    double *frus = xmalloc(sizeof(double) * 5 * n);
+    int *ltype = xmalloc(sizeof(int) * 8 * n), *ryr = xmalloc(sizeof(int) * 20 * n), *ito2 = xmalloc(sizeof(int) * 4 * n);
     FILE *fs, *ff, *fl, *fr, *fi;
     int j, k, q;
     if (!frus || !ltype || !ryr || !ito2 || gw_download(ctx, frus, ltype, ryr, ito2, NULL, NULL)) {
@@ -348,10 +370,10 @@ static void write_exact(const run_cfg *c, int num, int filenumber, double time, 
     exact_header h;
     char path[1200];
     FILE *f;
-    double *frus = malloc(sizeof(double) * 5 * n);
-    int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n), *ito2 = malloc(sizeof(int) * 4 * n);
-    int *mti = malloc(sizeof(int) * n);
-    uint32_t *mt = malloc(sizeof(uint32_t) * 624 * (size_t)n);
+    double *frus = xmalloc(sizeof(double) * 5 * n);
+    int *ltype = xmalloc(sizeof(int) * 8 * n), *ryr = xmalloc(sizeof(int) * 20 * n), *ito2 = xmalloc(sizeof(int) * 4 * n);
+    int *mti = xmalloc(sizeof(int) * n);
+    uint32_t *mt = xmalloc(sizeof(uint32_t) * 624 * (size_t)n);
     int bad;
     if (!frus || !ltype || !ryr || !ito2 || !mti || !mt || gw_download(ctx, frus, ltype, ryr, ito2, mti, mt)) {
         fprintf(stderr, "exact checkpoint: download failed: %s\n", gw_last_error());
@@ -390,10 +412,10 @@ static void read_exact(run_cfg *c, gw_ctx *ctx, double *state, double *time, dou
     const int n = c->nfru;
     exact_header h;
     FILE *f = fopen(c->restart_file, "rb");
-    double *frus = malloc(sizeof(double) * 5 * n);
-    int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n), *ito2 = malloc(sizeof(int) * 4 * n);
-    int *mti = malloc(sizeof(int) * n);
-    uint32_t *mt = malloc(sizeof(uint32_t) * 624 * (size_t)n);
+    double *frus = xmalloc(sizeof(double) * 5 * n);
+    int *ltype = xmalloc(sizeof(int) * 8 * n), *ryr = xmalloc(sizeof(int) * 20 * n), *ito2 = xmalloc(sizeof(int) * 4 * n);
+    int *mti = xmalloc(sizeof(int) * n);
+    uint32_t *mt = xmalloc(sizeof(uint32_t) * 624 * (size_t)n);
     if (!f) {
         fprintf(stderr, "Cannot open file '%s'!\n", c->restart_file);
         exit(2);
@@ -556,10 +578,10 @@ static void init_cell(const run_cfg *c, gw_ctx *ctx, double *state)
         return;
     }
     {
-        double *frus = malloc(sizeof(double) * 5 * n), a1 = 0.0, a2 = 0.0;
-        int *ltype = malloc(sizeof(int) * 8 * n), *ryr = malloc(sizeof(int) * 20 * n);
-        int *ito2 = malloc(sizeof(int) * 4 * n), *mti = malloc(sizeof(int) * n), j, q, k;
-        uint32_t *mt = calloc((size_t)624 * n, sizeof(uint32_t));
+        double *frus = xmalloc(sizeof(double) * 5 * n), a1 = 0.0, a2 = 0.0;
+        int *ltype = xmalloc(sizeof(int) * 8 * n), *ryr = xmalloc(sizeof(int) * 20 * n);
+        int *ito2 = xmalloc(sizeof(int) * 4 * n), *mti = xmalloc(sizeof(int) * n), j, q, k;
+        uint32_t *mt = xcalloc((size_t)624 * n, sizeof(uint32_t));
         read_ic(c, state, frus, ltype, ryr, ito2);
         if (c->reset_RyRs_flag)  /* initialize_state.c:252-263: every LCC closed and available, every RyR in 1 */
             for (j = 0; j < n; j++)
@@ -648,12 +670,12 @@ int main(int argc, char **argv)
             exit(-4);
         }
         props.n = c.fru_end - c.fru_start + 1;
-        props.fru = malloc(sizeof(FILE *) * props.n);
-        props.avg = malloc(sizeof(FILE *) * props.n);
-        props.frus = malloc(sizeof(double) * 5 * props.n);
-        props.ltype = malloc(sizeof(int) * 8 * props.n);
-        props.ryr = malloc(sizeof(int) * 20 * props.n);
-        props.ito2 = malloc(sizeof(int) * 4 * props.n);
+        props.fru = xmalloc(sizeof(FILE *) * props.n);
+        props.avg = xmalloc(sizeof(FILE *) * props.n);
+        props.frus = xmalloc(sizeof(double) * 5 * props.n);
+        props.ltype = xmalloc(sizeof(int) * 8 * props.n);
+        props.ryr = xmalloc(sizeof(int) * 20 * props.n);
+        props.ito2 = xmalloc(sizeof(int) * 4 * props.n);
         if (!props.fru || !props.avg || !props.frus || !props.ltype || !props.ryr || !props.ito2) {
             fprintf(stderr, "write_fru_props: out of host memory\n");
             exit(4);
