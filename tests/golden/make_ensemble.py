@@ -1,11 +1,12 @@
-"""Ensemble fixture from the reference program: 64 seeds of the NFRU=250 cell,
-rest state, 1 Hz pacing, first beat (1000 ms).  Seed k gives FRU j the MT19937
+"""Ensemble fixture from the reference program: 64 seeds of the NFRU=250 cell
+(ensemble250.npz; `--nfru N` for ensembleN.npz), rest state, 1 Hz pacing,
+first beat (1000 ms).  Seed k gives FRU j the MT19937
 seed 5489 + 100000*k + j.  Stores per-ms ensemble mean and standard deviation
 of V, Cai, mean CaJSR and the LCC / RyR open probabilities, plus each seed's
 peak Cai and APD90 (90% repolarisation after the 10-ms stimulus).
 
 Runs the 64 reference programs in parallel (oracle/_ref, built from the
-reference's sources); about 45 CPU-minutes.
+reference's sources); about 45 CPU-minutes at 250 FRUs, 5x that at 1250.
 """
 import os
 import sys
@@ -37,8 +38,9 @@ def apd90(t, v):
     return float(t[i0 + after[0]] - t[up])
 
 
-def one(k):
-    d = build_ref.build_config("ens_%d" % NFRU, build_ref.cfg_macros(NFRU, T_END))
+def one(job):
+    k, nfru = job
+    d = build_ref.build_config("ens_%d" % nfru, build_ref.cfg_macros(nfru, T_END))
     with tempfile.TemporaryDirectory() as tmp:
         build_ref.run_stoch(d, tmp, seed_base=seed_base(k))
         st = np.loadtxt(os.path.join(tmp, "states.0.txt"), skiprows=1)
@@ -60,12 +62,16 @@ def summarise(states, others):
 
 
 if __name__ == "__main__":
-    build_ref.build_config("ens_%d" % NFRU, build_ref.cfg_macros(NFRU, T_END))
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nfru", type=int, default=NFRU)
+    nfru = ap.parse_args().nfru
+    build_ref.build_config("ens_%d" % nfru, build_ref.cfg_macros(nfru, T_END))
     with ProcessPoolExecutor(max_workers=os.cpu_count()) as ex:
-        res = sorted(ex.map(one, range(NSEED)))
+        res = sorted(ex.map(one, [(k, nfru) for k in range(NSEED)]))
     states = np.array([r[1] for r in res])
     others = np.array([r[2] for r in res])
     out = summarise(states, others)
-    out.update(nseed=np.array([NSEED]), nfru=np.array([NFRU]), seed_stride=np.array([100000]))
-    np.savez_compressed(os.path.join(HERE, "ensemble250.npz"), **out)
+    out.update(nseed=np.array([NSEED]), nfru=np.array([nfru]), seed_stride=np.array([100000]))
+    np.savez_compressed(os.path.join(HERE, "ensemble%d.npz" % nfru), **out)
     print("apd90 mean %.2f ms, peak Cai mean %.4g mM" % (np.nanmean(out["apd90"]), out["peak_Cai"].mean()))
