@@ -285,3 +285,20 @@ def test_exact_restart_rejects_wrong_size(tmp_path):
                         "restart_file=%s" % (tmp_path / "a" / "r_exact.0.bin")], cwd=tmp_path, capture_output=True,
                        text=True)
     assert r.returncode != 0 and "holds 64 FRUs" in r.stderr
+
+
+def test_golden_driver_cases_match_their_generator():
+    """The driver settings the tests use for tests/golden/drv250* are the ones
+    tests/golden/make_driver_files.py made the files with."""
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_driver_files as mdf
+    assert sorted(GOLDEN_DRIVER_CASES) == sorted(mdf.CASES)
+    for name, (time_end, vclamp) in mdf.CASES.items():
+        args = golden_driver_args(name)
+        assert args["time_end"] == time_end and args["NFRU_sim"] == mdf.NFRU and args["seed_base"] == mdf.SEED_BASE
+        if vclamp:
+            assert args["vclamp_flag"] == 1
+            for k, v in vclamp.items():
+                assert args["vclamp_" + k] == v, k
+        else:
+            assert "vclamp_flag" not in args
