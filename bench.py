@@ -7,37 +7,41 @@ statistics): `value` is the throughput of an ensemble of --seeds cells (cell
 k's FRU j seeded 5489 + 100000 k + j) running on the GPU at once, one stream
 and one host integrator thread per cell -- the same kind of throughput the
 reference arm measures with one cell per host core, and the same number of
-cells (16) as that arm runs on the host's 16 cores.  With packed launches
-(16-64 FRUs per warp, each cell a few hundred warps) more cells fill more of
-the FP64 pipe: 4, 8 and 16 cells gave 51.4, 51.7 and 70.4 cell-ms/s (the 8-cell
-figure over the heavier [30, 130) ms).  A step advances every cell by STEP_MS (10 ms) of
-simulated time through the whole hot path (Dormand-Prince global step, every
-FRU stage on the GPU).  Warm-up steps cover [0, W*10) ms (the stimulus and
-upstroke), so with the defaults (W=3, K=20) the timed window is [30, 230) ms:
-the plateau and early repolarisation of the first beat.  L2 (129 MB) is
-flushed by a 512 MB write between timed steps.  Each step is timed on the
-device (events on a timing stream joined to every cell's stream).
+cells (16) as that arm runs on the host's 16 cores.  A step advances every
+cell by STEP_MS (10 ms) of simulated time through the whole hot path
+(Dormand-Prince global step, every FRU stage on the GPU).
 
-Beside it the line carries one cell alone ("one_cell": the latency of the
-plain method, CUDA events on its stream), the same window in mixed precision
-("mixed", with its error against the FP64 run), a batched run ("batched": 64
-cells of NFRU 1250-12,500 with varied pacing and conductances running
-concurrently, mixed precision) and a serving sweep ("serving": Poisson
+The timed window is pinned: every section first advances its cells from
+rest through the stimulus and upstroke to 30 ms (untimed set-up), keeps
+their complete state on the host, runs the W warm-up steps, puts the state
+back and tunes the launch shape, so the K timed steps always cover [30,
+30 + 10 K) ms -- [30, 230) ms by default, the plateau and early
+repolarisation of the first beat -- whatever W is.  L2 (129 MB) is flushed by
+a 512 MB write between timed steps.  Each step is timed on the device
+(events on a timing stream joined to every cell's stream).
+
+Beside it the line carries the same ensemble in mixed precision over the
+same window ("mixed_ensemble", with its speed-up and its paired error against
+the FP64 ensemble: peak Cai with a 95% interval, ensemble-mean V, JSR
+depletion, open probabilities), one cell alone ("one_cell", "mixed"), a
+batched run ("batched": 64 cells of NFRU 1250-12,500 with varied pacing and
+conductances, mixed precision) and a serving sweep ("serving": Poisson
 arrivals of cell requests, p50/p99 latency).  Before each timed section the
 launch-shape autotuner picks lanes per FRU and warps per block on the
-section's own workload ("tuning"; results do not depend on the choice).
+section's own workload ("tuning"; results do not depend on the choice), and
+`roofline.kernel` names the stage kernel it picked.
 
-value: inputs resident in HBM.  e2e: the ensemble's window through the C-ABI
-with host buffers: every step uploads each cell's full FRU + RNG state from
-host memory (gw_upload) and downloads it and the step's traces (gw_download)
-inside the timed region.
+value: inputs resident in HBM.  e2e: the ensemble's window again through the
+C-ABI with host buffers, on the same cells put back to 30 ms: every step
+uploads each cell's full FRU + RNG state from host memory (gw_upload) and
+downloads it and the step's traces (gw_download) inside the timed region.
 
 --impl reference: the reference's own serial program (oracle/_ref, built
 from its sources) on the host cores, one independent 12,500-FRU cell per
-core, each step a bounded 1-ms sample per cell starting from the bench
-cell's state at 30, 80, 130 or 180 ms (tests/golden/ic_window), i.e. the
-phases of the timed window.  cpu_baseline: the same program on one core,
-1 ms from each of those four states.
+core; timed step s runs every core for 3 simulated ms from the bench cell's
+state at phase s mod 10 of the same window (30, 50, ..., 210 ms;
+tests/golden/ic_window), so K = 20 steps sample each phase twice.
+cpu_baseline: the same program on one core, 1 ms from each of those phases.
 """
 import argparse
 import json
@@ -55,13 +59,31 @@ sys.path.insert(0, ROOT)
 NFRU = 12500
 STEP_MS = 10.0
 SEED = 5489
+# The timed window starts here whatever --warmup is: every section first
+# advances its cells from rest through the stimulus (10 ms) and the upstroke
+# (untimed set-up), keeps their state, runs the warm-up steps, and puts the
+# state back before the timed steps, so the GPU arm and the reference arm's
+# phase samples cover the same simulated window, [30, 30 + 10 K) ms.
+WINDOW_START_MS = 30.0
+# simulated ms per reference cell per timed step (the process start-up,
+# ~0.06 s, is then under 1% of a sample; 16 Arm cores run a 20-step sample of
+# the window in about 3 minutes)
+REF_SAMPLE_MS = 3.0
+# two-sided 95% quantile of Student's t for n - 1 degrees of freedom
+T975 = {1: 12.706, 2: 4.303, 3: 3.182, 4: 2.776, 5: 2.571, 6: 2.447, 7: 2.365, 8: 2.306, 9: 2.262, 10: 2.228,
+        11: 2.201, 12: 2.179, 13: 2.160, 14: 2.145, 15: 2.131, 16: 2.120, 17: 2.110, 18: 2.101, 19: 2.093,
+        20: 2.086, 24: 2.064, 30: 2.042, 40: 2.021, 63: 1.998, 127: 1.979, 255: 1.969}
 # algorithmic work per FRU-substep (static count of the reference's substep:
 # fru_rates_local + 2 x fcn_fru + simfru_local body, each add/mul/div/exp/
 # compare/convert counted once) and MT19937 bytes streamed per substep
-# DRAM bytes per stage launch of a 12,500-FRU cell: ncu's dram__bytes_read +
-# dram__bytes_write of a 2,500-FRU plateau launch (6.67 MB, cold L2 per
-# replay) times 5 (the bytes are per FRU: its state and MT row).
-TRAFFIC_PER_LAUNCH_12500 = 5 * 6.672128e6
+# DRAM bytes per stage launch of a 12,500-FRU cell, by kernel, from ncu's
+# dram__bytes_read + dram__bytes_write (profiles/): the fixed-layout FP64
+# kernel's 2,500-FRU plateau launch (6.67 MB, cold L2 per replay) times 5
+# (the bytes are per FRU: its state and MT row).
+TRAFFIC_PER_LAUNCH = {
+    "fru_stage4_kernel": (5 * 6.672128e6, "ncu dram bytes of one 2,500-FRU plateau launch x 5 (cold L2 per replay; "
+                                          "profiles/fru_stage4_kernel_plateau_2500fru.md)"),
+}
 FLOPS_PER_SUBSTEP = 700.0
 BYTES_PER_SUBSTEP = 384.0
 # GB300 FP32 (non-tensor) peak, nominal: 152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz
@@ -110,6 +132,9 @@ def parse():
                     help="only run the mixed-vs-FP64 ensemble check: SEEDS 12,500-FRU cells per precision "
                          "over [0, MS) ms, APD90 / peak Cai / JSR depletion / open probabilities")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--only-ensemble", action="store_true",
+                    help="run the headline ensemble section alone (for launch lists: its timed launches are the run's "
+                         "last `gpu_launches` launches)")
     ap.add_argument("--packed", type=int, default=0,
                     help="force packed launches with 1/N as many warps as 8-FRU groups (no autotuning)")
     ap.add_argument("--tune-ms", type=float, default=2.0, help="simulated window per autotuner candidate")
@@ -226,10 +251,26 @@ def reference_build(ms, window_ic=False):
         return None, "reference build failed: %s" % str(e).splitlines()[0]
 
 
-def window_phases():
+def window_phases(args=None):
+    """IC directories of the bench cell's state at phases of the timed window
+    (tests/golden/ic_window/t<ms>), sorted by time; with args, only those
+    inside [WINDOW_START_MS, WINDOW_START_MS + steps * step_ms)."""
     if not os.path.isdir(WINDOW_IC):
         return []
-    return [os.path.join(WINDOW_IC, d) for d in sorted(os.listdir(WINDOW_IC), key=lambda d: float(d[1:]))]
+    ds = sorted(os.listdir(WINDOW_IC), key=lambda d: float(d[1:]))
+    if args is not None:
+        lo, hi = window_ms(args)
+        ds = [d for d in ds if lo <= float(d[1:]) < hi]
+    return [os.path.join(WINDOW_IC, d) for d in ds]
+
+
+def window_ms(args):
+    """The timed window: it starts at WINDOW_START_MS whatever --warmup is."""
+    return WINDOW_START_MS, WINDOW_START_MS + args.steps * args.step_ms
+
+
+def window_str(args):
+    return "[%g, %g) ms" % window_ms(args)
 
 
 def reference_sample(d, procs, ms, seed0, phases=None):
@@ -266,38 +307,46 @@ def reference_sample(d, procs, ms, seed0, phases=None):
 
 def run_reference(args, dist):
     """The reference program on all host cores, one independent 12,500-FRU cell
-    per core, each step 1 simulated ms per cell.  The cells start from the
-    bench cell's state at 30, 80, 130 and 180 ms (tests/golden/ic_window, in
-    turn), so the sample covers the phases of the GPU arm's timed window
-    rather than the cheaper rest state."""
+    per core.  Timed step s runs every core from the bench cell's state at
+    phase s mod P of the GPU arm's timed window (P phases 20 ms apart,
+    tests/golden/ic_window) for REF_SAMPLE_MS simulated ms, each core with
+    its own seeds; over K = 20 steps every phase of [30, 230) ms is sampled
+    twice.  All cores of a step start from the same phase, so none idles
+    behind a costlier one.  Warm-up steps (nothing to warm on the host) are
+    1-ms samples of the first phase."""
     if dist.rank != 0:
         return
-    ms = 1.0
-    phases = window_phases()
-    d, why = reference_build(ms, window_ic=bool(phases))
-    if d is None:
-        print(json.dumps({"impl": "reference", "unavailable": why}))
+    phases = window_phases(args)
+    d, why = reference_build(REF_SAMPLE_MS, window_ic=bool(phases))
+    d1, why1 = reference_build(1.0, window_ic=bool(phases))
+    if d is None or d1 is None:
+        print(json.dumps({"impl": "reference", "unavailable": why or why1}))
         return
     procs = os.cpu_count() or 1
     for _ in range(args.warmup):
-        reference_sample(d, procs, ms, SEED, phases)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        reference_sample(d, procs, ms, SEED, phases)
-    wall = time.perf_counter() - t0
-    value = args.steps * procs * ms / wall
-    start = ("from the bench cell's state at %s ms (IC files, first 1250 FRUs replicated as the reference "
-             "reads them)" % "/".join(os.path.basename(p)[1:] for p in phases)) if phases else "from rest"
+        reference_sample(d1, procs, 1.0, SEED, phases[:1])
+    wall = 0.0
+    visits = {}
+    for k in range(args.steps):
+        ph = phases[k % len(phases)] if phases else None
+        wall += reference_sample(d, procs, REF_SAMPLE_MS, SEED + 1000003 * k, [ph])[1]
+        if ph:
+            visits[os.path.basename(ph)[1:]] = visits.get(os.path.basename(ph)[1:], 0) + 1
+    value = args.steps * procs * REF_SAMPLE_MS / wall
+    start = ("from the bench cell's state at %s ms (IC files; the reference reads 1250 FRUs and replicates them to "
+             "12,500), visits per phase %s" % ("/".join(os.path.basename(p)[1:] for p in phases),
+                                                json.dumps(visits, sort_keys=True))) if phases else "from rest"
     sample = ("reference program (caf.c, serial build of its own sources, gcc -O3) x%d concurrent cells, "
-              "NFRU=12,500 each, 1 ms per cell per step, %s" % (procs, start))
+              "NFRU=12,500 each, %g ms per cell per step, %s" % (procs, REF_SAMPLE_MS, start))
     print(json.dumps({
         "impl": "reference", "metric": "cell-ms simulated/s at 12,500 FRUs", "value": value,
         "unit": "cell-ms/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "one 12,500-FRU cell per host core, 1 Hz pacing, seeds 5489+j, 1-ms samples of "
-                               "the phases of the window [30, 230) ms",
-                   "nfru": NFRU, "cells": procs, "ms_per_cell_per_step": ms},
+        "config": {"workload": "one 12,500-FRU cell per host core, 1 Hz pacing, %g-ms samples of the phases of the "
+                               "timed window %s (the window the GPU arm times)" % (REF_SAMPLE_MS, window_str(args)),
+                   "window": window_str(args), "nfru": NFRU, "cells": procs, "ms_per_cell_per_step": REF_SAMPLE_MS,
+                   "phases_ms": [float(os.path.basename(p)[1:]) for p in phases]},
         "cpu_baseline": {"value": value, "unit": "cell-ms/s", "cores": procs, "kind": "reference",
                          "sample": sample},
         "e2e": {"value": value, "unit": "cell-ms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -361,19 +410,38 @@ def apply_tuning(cell, tuning):
     cell.set_stage_packing(((cell.nfru + 7) // 8 + div - 1) // div if div else 0)
 
 
+def snapshot(cells, t, states, old):
+    """Host copy of the cells' complete state (FRU Ca, channels, MT19937 rows
+    and positions) and of their global states, clocks and step sizes."""
+    return [c.download() for c in cells], t.copy(), states.copy(), old.copy()
+
+
+def restore(cells, snap, t, states, old):
+    for c, h in zip(cells, snap[0]):
+        c.upload(h)
+    t[:] = snap[1]
+    states[:] = snap[2]
+    old[:] = snap[3]
+
+
 def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
-    """Device-resident run of one cell: warm-up, then K timed steps with CUDA
-    events on the library's stream.  Returns the measurements."""
+    """One cell alone: set-up to the window start, warm-up steps, state put
+    back, launch shape tuned, then K timed steps with CUDA events on the
+    library's stream.  Returns the measurements."""
     import numpy as np
     cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, precision)
-    t = 0.0
-    oldstep = st.step_max
     n = int(args.step_ms)
+    t, _, _, _ = cell.run(state, 0.0, int(WINDOW_START_MS), st.step_max, st, want=())
+    t = np.array([t])
+    states = state[None, :]
+    old = np.array([cell.oldstep])
+    snap = snapshot([cell], t, states, old)
     for _ in range(args.warmup):
-        t, _, _, _ = cell.run(state, t, n, oldstep, st, want=())
-        oldstep = cell.oldstep
+        t[0], _, _, _ = cell.run(states[0], t[0], n, old[0], st, want=())
+        old[0] = cell.oldstep
+    restore([cell], snap, t, states, old)
     # launch shape picked on this cell's own workload (same results either way)
-    tuning = choose_shape(G, args, [cell], [st], np.array([t]), state[None, :].copy(), np.array([oldstep]))
+    tuning = choose_shape(G, args, [cell], [st], t, states.copy(), old)
     sub0, launch0 = cell.substeps(), cell.launches()
     cell.profile(True)
     total_ms = 0.0
@@ -385,12 +453,12 @@ def time_single(G, args, dist, precision, seed, keep_trace=False, clocks=None):
     for _ in range(args.steps):
         cell.l2_flush()
         cell.event(0)
-        t, states, _, _ = cell.run(state, t, n, oldstep, st, want=("states",) if keep_trace else ())
-        oldstep = cell.oldstep
+        t[0], tr, _, _ = cell.run(states[0], t[0], n, old[0], st, want=("states",) if keep_trace else ())
+        old[0] = cell.oldstep
         cell.event(1)
         total_ms += cell.elapsed_ms(0, 1)
         if keep_trace:
-            trace.append(states)
+            trace.append(tr)
     cell.sync()
     clk = clocks.stop() if clocks else None
     dist.barrier()
@@ -417,12 +485,15 @@ def ensemble(G, args, dist, precision):
     return cells, sets, np.ascontiguousarray(np.array(states))
 
 
-def time_ensemble(G, args, dist, precision, clocks=None):
+def time_ensemble(G, args, dist, precision, clocks=None, traces=False, e2e=False):
     """The ensemble on the GPU at once (one stream and host driver thread per
-    cell): W warm-up steps, the launch-shape autotuner, then K timed steps,
-    each timed on the device from before the first cell's first launch to
-    after the last cell's last one (gw_group_timer), L2 flushed between
-    steps."""
+    cell): set-up from rest to the window start, W warm-up steps, the state
+    put back, the launch-shape autotuner, then K timed steps, each timed on
+    the device from before the first cell's first launch to after the last
+    cell's last one (gw_group_timer), L2 flushed between steps.  traces:
+    also return each cell's per-ms global states and output averages from 0
+    ms to the window's end.  e2e: then the same window again through the
+    C-ABI with host buffers (time_e2e_steps)."""
     import numpy as np
     cells, sets, states = ensemble(G, args, dist, precision)
     n = len(cells)
@@ -430,8 +501,12 @@ def time_ensemble(G, args, dist, precision, clocks=None):
     old = np.full(n, 0.1)
     runner = G.Batch(precision)
     step = int(args.step_ms)
+    tr = runner.run(cells, sets, t, states, old, int(WINDOW_START_MS), traces=traces, lockstep=False)
+    st_parts, ot_parts = ([tr[0]], [tr[1]]) if traces else ([], [])
+    snap = snapshot(cells, t, states, old)
     for _ in range(args.warmup):
         runner.run(cells, sets, t, states, old, step, lockstep=False)
+    restore(cells, snap, t, states, old)
     tuning = choose_shape(G, args, cells, sets, t, states, old)
     sub0 = sum(c.substeps() for c in cells)
     launch0 = sum(c.launches() for c in cells)
@@ -445,38 +520,40 @@ def time_ensemble(G, args, dist, precision, clocks=None):
     for _ in range(args.steps):
         cells[0].l2_flush()
         timer.start()
-        runner.run(cells, sets, t, states, old, step, lockstep=False)
+        tr = runner.run(cells, sets, t, states, old, step, traces=traces, lockstep=False)
         total_ms += timer.stop()
+        if traces:
+            st_parts.append(tr[0])
+            ot_parts.append(tr[1])
     clk = clocks.stop() if clocks else None
     dist.barrier()
     out = {"device_ms": dist.max(total_ms), "substeps": sum(c.substeps() for c in cells) - sub0,
-           "launches": sum(c.launches() for c in cells) - launch0, "clocks": clk, "tuning": tuning, "cells": n}
+           "launches": sum(c.launches() for c in cells) - launch0, "clocks": clk, "tuning": tuning, "cells": n,
+           "window": window_str(args)}
     out["value"] = dist.sum(n * args.steps * args.step_ms) / (out["device_ms"] / 1000.0)
+    if traces:
+        out["state_trace"] = np.concatenate(st_parts, axis=1)
+        out["other_trace"] = np.concatenate(ot_parts, axis=1)
+    if e2e:
+        out["e2e"] = time_e2e_steps(args, dist, cells, sets, runner, snap, t, states, old)
     for c in cells:
         c.close()
     runner.close()
     return out
 
 
-def time_ensemble_e2e(G, args, dist, precision, tuning=None):
-    """The ensemble's timed window through the C-ABI with host buffers: every
-    step uploads each cell's full FRU + RNG state and global state from host
-    memory, runs the step, and downloads them and the step's traces."""
+def time_e2e_steps(args, dist, cells, sets, runner, snap, t, states, old):
+    """The ensemble's timed window through the C-ABI with host buffers, on the
+    same (warm) cells put back to the window start: every step uploads each
+    cell's full FRU + RNG state and global state from host memory, runs the
+    step, and downloads them and the step's traces."""
     import numpy as np
-    cells, sets, states = ensemble(G, args, dist, precision)
-    n = len(cells)
-    if tuning:
-        for c in cells:
-            apply_tuning(c, tuning)
-    t = np.zeros(n)
-    old = np.full(n, 0.1)
-    runner = G.Batch(precision)
-    step = int(args.step_ms)
-    for _ in range(args.warmup):
-        runner.run(cells, sets, t, states, old, step, lockstep=False)
-    host = [c.download() for c in cells]
-    h_states = states.copy()
+    restore(cells, snap, t, states, old)
+    host = [dict(h) for h in snap[0]]
+    h_states = snap[2].copy()
     h2d = sum(v.nbytes for h in host for v in h.values()) + h_states.nbytes
+    n = len(cells)
+    step = int(args.step_ms)
     dist.barrier()
     e2e_s, d2h = 0.0, 0
     for _ in range(args.steps):
@@ -489,44 +566,41 @@ def time_ensemble_e2e(G, args, dist, precision, tuning=None):
         e2e_s += time.perf_counter() - t0
         d2h = sum(v.nbytes for h in host for v in h.values()) + st_tr.nbytes + ot_tr.nbytes
     dist.barrier()
-    for c in cells:
-        c.close()
-    runner.close()
     return {"value": dist.sum(n * args.steps * args.step_ms) / dist.max(e2e_s), "unit": "cell-ms/s",
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "window": window_str(args)}
 
 
-def time_e2e(G, args, dist, seed, tuning=None):
-    """The same window through the C-ABI with host buffers: the cell's full FRU +
-    RNG state is uploaded and downloaded, and its traces read back, every step."""
-    cell, st, state = fresh_cell(G, args.nfru, seed, args.fru_lanes, args.precision)
-    if tuning:
-        apply_tuning(cell, tuning)
-    t = 0.0
-    oldstep = st.step_max
-    n = int(args.step_ms)
-    for _ in range(args.warmup):
-        t, _, _, _ = cell.run(state, t, n, oldstep, st, want=())
-        oldstep = cell.oldstep
-    host = cell.download()
-    h_state = state.copy()
-    h2d = sum(v.nbytes for v in host.values()) + h_state.nbytes
-    dist.barrier()
-    cell.sync()
-    e2e_ms, d2h = 0.0, 0
-    for _ in range(args.steps):
-        cell.l2_flush()
-        t0 = time.perf_counter()
-        cell.upload(host)
-        t, states, other, cur = cell.run(h_state, t, n, oldstep, st)
-        oldstep = cell.oldstep
-        host = cell.download()
-        e2e_ms += (time.perf_counter() - t0) * 1000.0
-        d2h = sum(v.nbytes for v in host.values()) + states.nbytes + other.nbytes + cur.nbytes
-    dist.barrier()
-    cell.close()
-    return {"value": dist.sum(args.steps * args.step_ms) / (dist.max(e2e_ms) / 1000.0), "unit": "cell-ms/s",
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+def paired_ci(a, b):
+    """Mean of the paired differences b - a relative to mean(a), with its 95%
+    interval (Student's t, n - 1 degrees of freedom)."""
+    import numpy as np
+    d = np.asarray(b, float) - np.asarray(a, float)
+    n = len(d)
+    ref = float(np.mean(a))
+    m = float(d.mean()) / ref
+    if n < 2:
+        return {"rel_mean_diff": m, "ci95": None, "n": n}
+    tq = T975.get(n - 1) or T975[max(k for k in T975 if k <= n - 1)]
+    h = tq * float(d.std(ddof=1)) / np.sqrt(n) / abs(ref)
+    return {"rel_mean_diff": m, "ci95": [m - h, m + h], "n": n, "within_1pct": bool(abs(m) + h < 0.01)}
+
+
+def precision_vs_fp64(f, m):
+    """Mixed precision against the FP64 run of the same seeds over [0, window
+    end): per-seed peak Cai (paired, 95% interval), ensemble-mean V, JSR
+    depletion and the LCC / RyR open-probability traces."""
+    import numpy as np
+    fs, ms_ = f["state_trace"], m["state_trace"]
+    fo, mo = f["other_trace"], m["other_trace"]
+    pk_f, pk_m = fs[:, :, 6].max(1), ms_[:, :, 6].max(1)
+    return {"seeds": int(fs.shape[0]), "window_ms": [0, int(fs.shape[1])],
+            "peak_cai": dict(paired_ci(pk_f, pk_m), fp64_mean_mM=float(pk_f.mean()), mixed_mean_mM=float(pk_m.mean())),
+            "max_abs_d_ensemble_mean_V_mV": float(np.max(np.abs(ms_[:, :, 0].mean(0) - fs[:, :, 0].mean(0)))),
+            "jsr_depletion_rel_diff": float(mo[:, :, 1].mean(0).min() / fo[:, :, 1].mean(0).min() - 1.0),
+            "max_abs_d_p_lcc_open": float(np.max(np.abs(mo[:, :, 7].mean(0) - fo[:, :, 7].mean(0)))),
+            "max_abs_d_p_ryr_open": float(np.max(np.abs(mo[:, :, 3].mean(0) - fo[:, :, 3].mean(0)))),
+            "note": "APD90 needs the whole action potential (about 500 ms); it is in the longer precision study "
+                    "(bench.py --precision-ensemble)"}
 
 
 def batch_cells(G, args, dist):
@@ -690,7 +764,7 @@ def precision_ensemble(G, args, dist):
             for k in ks:
                 c = G.Cell(NFRU, precision=prec)
                 if prec == "fp64":
-                    c.set_stage_packing(((NFRU + 7) // 8 + 3) // 4)  # the FP64 ensemble's tuned shape
+                    c.set_stage_packing(((NFRU + 7) // 8 + 7) // 8)  # the FP64 ensemble's tuned shape
                 st = G.settings()
                 states.append(c.init_rest(st, scheme=G.SEED_BASE, base=SEED + 100000 * k))
                 cells.append(c)
@@ -718,13 +792,12 @@ def precision_ensemble(G, args, dist):
     ok = ~np.isnan(d_apd)  # seeds repolarised within the window in both runs
     fa, ma = f["apd90"][ok], m["apd90"][ok]
     return {"check": "precision_ensemble", "seeds": seeds, "window_ms": [0, ms], "nfru": NFRU,
-            "apd90_ms": {"fp64_mean": float(fa.mean()), "mixed_mean": float(ma.mean()),
-                         "rel_diff_of_means": float(ma.mean() / fa.mean() - 1.0),
-                         "paired_sem_rel": float(np.std(d_apd[ok], ddof=1) / np.sqrt(ok.sum()) / fa.mean()),
-                         "seeds_repolarised_in_both": int(ok.sum())},
-            "peak_cai_mM": {"fp64_mean": float(f["peak_cai"].mean()), "mixed_mean": float(m["peak_cai"].mean()),
-                            "rel_diff_of_means": float(m["peak_cai"].mean() / f["peak_cai"].mean() - 1.0),
-                            "paired_sem_rel": float(np.std(d_pk, ddof=1) / np.sqrt(seeds) / f["peak_cai"].mean())},
+            "apd90_ms": dict(paired_ci(fa, ma), fp64_mean=float(fa.mean()), mixed_mean=float(ma.mean()),
+                             paired_sem_rel=float(np.std(d_apd[ok], ddof=1) / np.sqrt(ok.sum()) / fa.mean()),
+                             seeds_repolarised_in_both=int(ok.sum())),
+            "peak_cai_mM": dict(paired_ci(f["peak_cai"], m["peak_cai"]), fp64_mean=float(f["peak_cai"].mean()),
+                                mixed_mean=float(m["peak_cai"].mean()),
+                                paired_sem_rel=float(np.std(d_pk, ddof=1) / np.sqrt(seeds) / f["peak_cai"].mean())),
             "jsr_depletion": {"fp64_min_mean_cajsr_mM": float(f["jsr"].min()), "mixed_min_mean_cajsr_mM": float(m["jsr"].min()),
                               "rel_diff": float(m["jsr"].min() / f["jsr"].min() - 1.0)},
             "open_probability_traces": {"max_abs_diff_lcc": float(np.max(np.abs(m["plcc"] - f["plcc"]))),
@@ -751,9 +824,18 @@ def run_gpu(args, dist):
         return
     seed = SEED + dist.rank * args.nfru  # replicas: independent streams per rank
     clocks = Clocks(dist.local)
-    # headline: the FP64 ensemble, all cells on the GPU at once
-    ens = time_ensemble(G, args, dist, args.precision, clocks=clocks)
+    want_mixed = args.precision == "fp64" and not args.no_mixed
+    # headline: the FP64 ensemble, all cells on the GPU at once; then the same
+    # window through the C-ABI with host buffers (e2e)
+    ens = time_ensemble(G, args, dist, args.precision, clocks=clocks, traces=want_mixed, e2e=not args.no_e2e)
     substeps = ens["substeps"]
+    if args.only_ensemble:
+        if dist.rank == 0:
+            print(json.dumps({"section": "ensemble only", "value": ens["value"], "unit": "cell-ms/s",
+                              "window": ens["window"], "gpu_launches": int(ens["launches"]),
+                              "kernel": stage_kernel_name(args.precision, ens["tuning"], args),
+                              "fru_substeps": int(substeps), "device_ms": ens["device_ms"], "tuning": ens["tuning"]}))
+        return
     # roofline of the dominant kernel (the FRU stage kernel, 98-99% of the
     # device time), FP64-pipe bound: algorithmic FLOPs of all its launches in
     # the timed region over the region's device time (the cells' launches
@@ -762,15 +844,25 @@ def run_gpu(args, dist):
     achieved_tf = FLOPS_PER_SUBSTEP * substeps / (ens["device_ms"] * 1e-3) / 1e12
     achieved_gbs = BYTES_PER_SUBSTEP * substeps / (ens["device_ms"] * 1e-3) / 1e9
     hbm_peak = load_peaks().get("hbm_gbs", 6800.0)
-    # one cell alone (the latency of the plain method; the denominator of the
-    # mixed, batched and serving speed-ups)
-    one = time_single(G, args, dist, args.precision, seed, keep_trace=True)
+    # the mixed-precision ensemble: the same seeds, cells and window
+    mixed_ens = None
+    if want_mixed:
+        m = time_ensemble(G, args, dist, "mixed", traces=True)
+        m_rate = m["substeps"] / (m["device_ms"] / 1000.0)
+        mixed_ens = {"value": m["value"], "unit": "cell-ms/s", "cells": m["cells"], "window": m["window"],
+                     "speedup_vs_fp64_ensemble": m["value"] / ens["value"], "fru_substeps_per_s": m_rate,
+                     "ms_per_step": m["device_ms"] / args.steps, "gpu_launches": int(m["launches"]),
+                     "kernel": stage_kernel_name("mixed", m["tuning"], args), "tuning": m["tuning"],
+                     "roofline": mixed_roofline(m_rate, hbm_peak), "clocks": None,
+                     "error_vs_fp64_same_seeds": precision_vs_fp64(ens, m)}
+        del m
+    # one cell alone (the latency of the plain method)
+    one = time_single(G, args, dist, args.precision, seed, keep_trace=want_mixed)
     one_line = {"value": one["value"], "unit": "cell-ms/s", "fru_substeps_per_s": one["substeps"] / (one["wall_ms"] / 1e3),
                 "per_launch_ms": one["kern_ms"] / max(one["kern_launches"], 1), "launches": int(one["kern_launches"]),
-                "tuning": one["tuning"], "timing": "CUDA events on the cell's stream"}
-
+                "tuning": one["tuning"], "timing": "CUDA events on the cell's stream", "window": window_str(args)}
     mixed = None
-    if args.precision == "fp64" and not args.no_mixed:
+    if want_mixed:
         m = time_single(G, args, dist, "mixed", seed, keep_trace=True)
         a, b = one["trace"], m["trace"]
         cai_range = float(np.max(a[:, 6]) - np.min(a[:, 6])) or 1.0
@@ -796,27 +888,28 @@ def run_gpu(args, dist):
                    "sweep": [time_serving(G, args, r) for r in args.serve_rates]}
         for r in serving["sweep"]:
             r["speedup_12500_equiv_vs_fp64_one_cell"] = r["cell_ms_per_s_12500_equiv"] / one["value"]
-    e2e = None if args.no_e2e else time_ensemble_e2e(G, args, dist, args.precision, ens["tuning"])
+    e2e = ens.get("e2e")
 
     # ---- CPU baseline: the reference program on one host core ----
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        phases = window_phases()
+        phases = window_phases(args)
         d, why = reference_build(1.0, window_ic=bool(phases))
         if d is not None:
             walls = [reference_sample(d, 1, 1.0, SEED, [ph])[1] for ph in (phases or [None])]
             v = len(walls) / sum(walls)
             cpu = {"value": v, "unit": "cell-ms/s", "cores": 1, "kind": "reference",
                    "sample": "reference program (serial build of its own sources), NFRU=12,500, 1 ms from the "
-                             "bench cell's state at each of %s ms of the timed window (%.1f s wall in all)"
-                             % ("/".join(os.path.basename(p)[1:] for p in phases) or "0", sum(walls))}
+                             "bench cell's state at each of %s ms of the timed window %s (%.1f s wall in all)"
+                             % ("/".join(os.path.basename(p)[1:] for p in phases) or "0", window_str(args),
+                                sum(walls))}
         else:
             cpu = {"value": None, "unit": "cell-ms/s", "cores": 0, "kind": "reference", "sample": why}
 
     if dist.rank == 0:
-        kernel = ("fru_stage_mixed_kernel" if args.precision == "mixed" else
-                  "fru_stage4_kernel" if args.fru_lanes == 4 else "fru_stage_kernel")
-        window = "[%g, %g) ms" % (args.warmup * args.step_ms, (args.warmup + args.steps) * args.step_ms)
+        kernel = stage_kernel_name(args.precision, ens["tuning"], args)
+        traffic = TRAFFIC_PER_LAUNCH.get(kernel) if args.nfru == NFRU else None
+        window = window_str(args)
         line = {
             "metric": "cell-ms simulated/s at 12,500 FRUs", "value": ens["value"], "unit": "cell-ms/s",
             "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
@@ -824,9 +917,10 @@ def run_gpu(args, dist):
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64", "data": "synthetic",
             "config": {"workload": "FP64 ensemble of %d cells per GPU (%d of the 64 seeds; cell k's FRU j seeded "
                                    "5489+100000k+j), NFRU=%d each, rest state, 1 Hz pacing (1 ms -100 uA/uF at 10 ms), "
-                                   "all cells on the GPU at once; step = %g ms simulated per cell; timed window %s"
-                                   % (args.seeds, args.seeds, args.nfru, args.step_ms, window),
-                       "nfru": args.nfru, "cells": args.seeds, "step_ms": args.step_ms,
+                                   "all cells on the GPU at once; step = %g ms simulated per cell; timed window %s "
+                                   "(fixed: untimed set-up from rest to %g ms, warm-up steps, state put back)"
+                                   % (args.seeds, args.seeds, args.nfru, args.step_ms, window, WINDOW_START_MS),
+                       "window": window, "nfru": args.nfru, "cells": args.seeds, "step_ms": args.step_ms,
                        "precision": ("fp64 (FRU path and global ODE)" if args.precision == "fp64" else
                                      "mixed (FRU rates and local Ca ODE fp32; FRU state, clock, flux sums "
                                      "and global ODE fp64)"),
@@ -841,9 +935,8 @@ def run_gpu(args, dist):
             "roofline": {"bound": "fp64", "kernel": kernel, "achieved": achieved_tf,
                          "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved_tf / fp64_peak if fp64_peak else None,
                          "peak_source": "measured in-run (independent DFMA chains on all SMs)",
-                         "traffic": TRAFFIC_PER_LAUNCH_12500 if args.nfru == NFRU else None,
-                         "traffic_note": "bytes per stage launch of a 12,500-FRU cell, from one ncu capture scaled "
-                                         "from 2,500 FRUs (cold L2 per replay; in the run the cells stay in L2)",
+                         "traffic": traffic[0] if traffic else None,
+                         "traffic_note": traffic[1] if traffic else "no ncu capture of this kernel on this workload",
                          "algorithmic": "%g FLOP per FRU-substep x %d FRU-substeps over the timed region's device time"
                                         % (FLOPS_PER_SUBSTEP, substeps),
                          "hbm_view": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
@@ -851,6 +944,7 @@ def run_gpu(args, dist):
                                       "algorithmic": "%g B x FRU-substeps" % BYTES_PER_SUBSTEP}},
             "clocks": ens["clocks"],
             "tuning": ens["tuning"],
+            "mixed_ensemble": mixed_ens,
             "one_cell": one_line,
             "mixed": mixed,
             "batched": batched,
@@ -859,6 +953,17 @@ def run_gpu(args, dist):
             "cpu_baseline": cpu,
         }
         print(json.dumps(line))
+
+
+def stage_kernel_name(precision, tuning, args):
+    """The FRU stage kernel a section's launches ran (the autotuner's choice)."""
+    packed = bool(tuning and tuning.get("packed_div"))
+    lanes = tuning["lanes_per_fru"] if tuning else args.fru_lanes
+    if precision == "mixed":
+        return "fru_stage_mixed_packed_kernel" if packed else "fru_stage_mixed_kernel"
+    if packed:
+        return "fru_stage4_packed_kernel"
+    return "fru_stage4_kernel" if lanes == 4 else "fru_stage_kernel"
 
 
 def main():

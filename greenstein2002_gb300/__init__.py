@@ -138,6 +138,7 @@ def bind(path):
         "gw_probe_fp64_peak": ([P(C.c_double)], C.c_int),
         "gw_probe_fcn": ([P(C.c_double), P(C.c_double)], C.c_int),
         "gw_probe_exp": ([_dp, _dp, _dp, C.c_int], C.c_int),
+        "gw_probe_fp64_issue": ([_dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name, None)
@@ -348,6 +349,26 @@ def fcn_cost_us(lib=None):
     d, h = C.c_double(0.0), C.c_double(0.0)
     _check(L.gw_probe_fcn(C.byref(d), C.byref(h)), "gw_probe_fcn", L)
     return d.value, h.value
+
+
+PROBE_ISSUE_CASES = (
+    "dependent DFMA, 1 warp, 32 active lanes", "dependent DFMA, 1 warp, 16 active lanes",
+    "dependent DFMA, 1 warp, 4 active lanes", "dependent DFMA, 1 warp, 1 active lane",
+    "dependent DFMA, 1 warp per SM", "dependent DFMA, 2 warps per SM", "dependent DFMA, 4 warps per SM",
+    "dependent DFMA, 8 warps per SM", "8 independent DFMA chains, 1 warp per SM (per DFMA per warp)",
+    "8 independent DFMA chains, 4 warps per SM (per DFMA per warp)",
+    "8 independent DFMA chains, 16 warps per SM (per DFMA per warp)", "dependent 1/x + c, 32 lanes",
+    "dependent 1/x + c, 1 lane", "dependent exp(), 32 lanes", "dependent exp(), 1 lane",
+    "dependent FFMA (FP32), 1 warp")
+
+
+def fp64_issue_cycles(lib=None):
+    """{case: cycles per operation} of the FP64 issue-cost chains on one SM
+    (gw_probe_fp64_issue, greenstein2002_gb300/csrc/gw_diag.h)."""
+    L = lib if lib is not None else load()
+    out = np.zeros(len(PROBE_ISSUE_CASES))
+    _check(L.gw_probe_fp64_issue(out), "gw_probe_fp64_issue", L)
+    return dict(zip(PROBE_ISSUE_CASES, out.tolist()))
 
 
 def fp64_peak_tflops():

@@ -11,6 +11,7 @@
 #include <new>
 #include <vector>
 
+#include "gw_diag.h"
 #include "gw_fru.h"
 #include "gw_kernels.h"
 #include "gw_fru_model.cuh"
@@ -567,6 +568,12 @@ extern "C" int gw_probe_fcn(double* device_us, double* host_us) {
 extern "C" int gw_probe_exp(const double* x, double* device_y, double* host_y, int n) {
   if (!x || !device_y || !host_y || n <= 0) return set_err(GW_EINVAL, "gw_probe_exp: bad argument");
   CK(gw::probe_exp(x, device_y, host_y, n));
+  return GW_OK;
+}
+
+extern "C" int gw_probe_fp64_issue(double* cycles) {
+  if (!cycles) return set_err(GW_EINVAL, "gw_probe_fp64_issue: null argument");
+  CK(gw::probe_fp64_issue(cycles));
   return GW_OK;
 }
 

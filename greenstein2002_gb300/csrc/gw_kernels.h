@@ -128,6 +128,8 @@ cudaError_t probe_fp64(int sms, double* tflops);
 cudaError_t probe_fcn(double* device_us, double* host_us);
 // exp of n arguments on the device and with the host libm.
 cudaError_t probe_exp(const double* x, double* device_y, double* host_y, int n);
+// FP64 issue-cost chains on one SM (gw_diag.h, gw_probe_fp64_issue).
+cudaError_t probe_fp64_issue(double* cycles);
 cudaError_t launch_seed(const DevState& s, int scheme, uint32_t base, cudaStream_t st);
 
 }  // namespace gw

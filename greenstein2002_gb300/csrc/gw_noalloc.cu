@@ -25,9 +25,29 @@ constexpr int kNoAllocMaxFru = 65536;
 constexpr int kNoAllocMaxBlocks = kNoAllocMaxFru / kStageThreads;
 constexpr size_t kNoAllocPartialsBytes = sizeof(double) * 5 * kNoAllocMaxBlocks;
 // out[] layout of this entry point: [0..4] flux sums, [5..8] Jxfer, Jtr,
-// ICa, Ito2, [9] error flag (substep limit reached)
+// ICa, Ito2, [9] error flag (1: substep limit reached; 2: an FRU's mti or a
+// channel state was out of range, and that FRU was left untouched)
 constexpr int kNoAllocOutError = 9;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocPartialsBytes + 256];
+
+// The caller's arrays do not pass through gw_upload's checks, so the kernel
+// checks what would otherwise index out of range: mti in 0..624 (the MT row)
+// and each cleft's channel word (LCC 1..12, VDI 1..2, RyR 1..8, ClCh 1..2;
+// the rate tables).
+__device__ __forceinline__ bool noalloc_valid(int mti, const uint32_t w[kClefts]) {
+  bool ok = mti >= 0 && mti <= kMtN;
+#pragma unroll
+  for (int c = 0; c < kClefts; c++) {
+    const int l = lcc_of(w[c]), v = vdi_of(w[c]), x = cl_of(w[c]);
+    ok = ok && l >= 1 && l <= 12 && v >= 1 && v <= 2 && x >= 1 && x <= 2;
+#pragma unroll
+    for (int i = 0; i < kRyR; i++) {
+      const int r = ryr_of(w[c], i);
+      ok = ok && r >= 1 && r <= 8;
+    }
+  }
+  return ok;
+}
 
 // Copy-on-twist is off here: the hold epoch word always equals the epoch the
 // kernel is launched with, so a regeneration never copies words aside (no
@@ -43,7 +63,7 @@ fru_stage_noalloc_kernel(int nfru, int stride, double* frus, uint32_t* chan, int
   __syncthreads();
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  bool overflow = false;
+  bool overflow = false, invalid = false;
   if (f < nfru) {
     const size_t nf = (size_t)stride;
     double y[5];
@@ -59,12 +79,15 @@ fru_stage_noalloc_kernel(int nfru, int stride, double* frus, uint32_t* chan, int
 #pragma unroll
     for (int c = 0; c < kClefts; c++) w[c] = chan[c * nf + f];
     rng.mti = mti[f];
-    advance_fru(p, y, w, rng, nsub, overflow);
+    invalid = !noalloc_valid(rng.mti, w);
+    if (!invalid) {
+      advance_fru(p, y, w, rng, nsub, overflow);
 #pragma unroll
-    for (int i = 0; i < 5; i++) frus[i * nf + f] = y[i];
+      for (int i = 0; i < 5; i++) frus[i * nf + f] = y[i];
 #pragma unroll
-    for (int c = 0; c < kClefts; c++) chan[c * nf + f] = w[c];
-    mti[f] = rng.mti;
+      for (int c = 0; c < kClefts; c++) chan[c * nf + f] = w[c];
+      mti[f] = rng.mti;
+    }
 #pragma unroll
     for (int c = 0; c < kClefts; c++) {
       v[0] += y[c + 1];
@@ -76,7 +99,8 @@ fru_stage_noalloc_kernel(int nfru, int stride, double* frus, uint32_t* chan, int
     }
     v[1] = y[0];
   }
-  if (overflow) out[kNoAllocOutError] = 1.0;
+  if (invalid) out[kNoAllocOutError] = 2.0;
+  else if (overflow) out[kNoAllocOutError] = 1.0;
   block_reduce<5>(v, smem);
   double tot[5];
   if (grid_finish<5>(v, partials, ticket, smem, tot)) {
@@ -123,7 +147,7 @@ extern "C" int gw_stage_noalloc(int nfru, int stride, double* frus, uint32_t* ch
   if (cudaMemsetAsync(ticket, 0, sizeof(unsigned), st) != cudaSuccess ||
       cudaMemsetAsync(out + kNoAllocOutError, 0, sizeof(double), st) != cudaSuccess)
     return gw_internal_error(GW_ECUDA, "gw_stage_noalloc: clearing the ticket failed");
-  StageParams p;
+  StageParams p = {};
   p.t0 = t0;
   p.tf = tf;
   for (int i = 0; i < 3; i++) {
@@ -132,6 +156,7 @@ extern "C" int gw_stage_noalloc(int nfru, int stride, double* frus, uint32_t* ch
     p.span[i] = depf[i] - dep0[i];
   }
   p.nfru_scale = nfru_scale;
+  p.pca_scale = 1.0;  // the reference PCa: this path runs the FP64 one-thread-per-FRU kernel only
   p.epoch = kNoHoldEpoch;
   p.flags = kFlagAdvance;
   const int nblocks = (nfru + kStageThreads - 1) / kStageThreads;

@@ -136,4 +136,113 @@ cudaError_t probe_exp(const double* x, double* device_y, double* host_y, int n) 
   return e;
 }
 
+// FP64 issue cost on one SM: clock64()-timed chains of 4096 dependent (or 8
+// independent) operations -- DFMA with 32/16/4/1 active lanes and 1-16 warps,
+// a DDIV+DADD chain, an exp() chain and an FP32 FFMA chain.  Each kernel runs
+// one block; out[1] receives warp 0's cycles per operation.
+__global__ void issue_dep_fma(double* out, int n, int active, double a, double b) {
+  if ((int)(threadIdx.x & 31) >= active) return;
+  double x = threadIdx.x * 1e-6;
+  const long long t0 = clock64();
+  for (int i = 0; i < n; i++) x = fma(x, a, b);
+  const long long t1 = clock64();
+  if (threadIdx.x == 0) {
+    out[0] = x;
+    out[1] = (double)(t1 - t0) / n;
+  } else if (x == 1.2345) {
+    out[2] = x;
+  }
+}
+__global__ void issue_ind_fma(double* out, int n, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  const long long t0 = clock64();
+  for (int i = 0; i < n; i++) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  const long long t1 = clock64();
+  const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (threadIdx.x == 0) {
+    out[0] = s;
+    out[1] = (double)(t1 - t0) / (8.0 * n);
+  } else if (s == 1.2345) {
+    out[2] = s;
+  }
+}
+__global__ void issue_dep_div(double* out, int n, int active) {
+  if ((int)(threadIdx.x & 31) >= active) return;
+  double x = 1.0 + threadIdx.x * 1e-6;
+  const long long t0 = clock64();
+  for (int i = 0; i < n; i++) x = 1.0000001 + 1.0 / x;
+  const long long t1 = clock64();
+  if (threadIdx.x == 0) {
+    out[0] = x;
+    out[1] = (double)(t1 - t0) / n;
+  } else if (x == 1.2345) {
+    out[2] = x;
+  }
+}
+__global__ void issue_dep_exp(double* out, int n, int active) {
+  if ((int)(threadIdx.x & 31) >= active) return;
+  double x = 0.1 + threadIdx.x * 1e-6;
+  const long long t0 = clock64();
+  for (int i = 0; i < n; i++) x = exp(-x);
+  const long long t1 = clock64();
+  if (threadIdx.x == 0) {
+    out[0] = x;
+    out[1] = (double)(t1 - t0) / n;
+  } else if (x == 1.2345) {
+    out[2] = x;
+  }
+}
+__global__ void issue_dep_ffma(double* out, int n, float a, float b) {
+  float x = threadIdx.x * 1e-6f;
+  const long long t0 = clock64();
+  for (int i = 0; i < n; i++) x = fmaf(x, a, b);
+  const long long t1 = clock64();
+  if (threadIdx.x == 0) {
+    out[0] = x;
+    out[1] = (double)(t1 - t0) / n;
+  } else if (x == 1.2345f) {
+    out[2] = x;
+  }
+}
+
+cudaError_t probe_fp64_issue(double* cycles) {
+  double* d = nullptr;
+  double h[3];
+  const int n = 4096;
+  cudaError_t e = cudaMalloc(&d, 3 * sizeof(double));
+  int k = 0;
+  auto take = [&]() {
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cycles[k++] = (e == cudaSuccess) ? h[1] : -1.0;
+  };
+  for (int act : {32, 16, 4, 1}) {
+    if (e == cudaSuccess) issue_dep_fma<<<1, 32>>>(d, n, act, 0.999999, 1e-7);
+    take();
+  }
+  for (int w : {1, 2, 4, 8}) {
+    if (e == cudaSuccess) issue_dep_fma<<<1, 32 * w>>>(d, n, 32, 0.999999, 1e-7);
+    take();
+  }
+  for (int w : {1, 4, 16}) {
+    if (e == cudaSuccess) issue_ind_fma<<<1, 32 * w>>>(d, n, 0.999999, 1e-7);
+    take();
+  }
+  for (int act : {32, 1}) {
+    if (e == cudaSuccess) issue_dep_div<<<1, 32>>>(d, n, act);
+    take();
+  }
+  for (int act : {32, 1}) {
+    if (e == cudaSuccess) issue_dep_exp<<<1, 32>>>(d, n, act);
+    take();
+  }
+  if (e == cudaSuccess) issue_dep_ffma<<<1, 32>>>(d, n, 0.999f, 1e-3f);
+  take();
+  cudaFree(d);
+  return e;
+}
+
 }  // namespace gw

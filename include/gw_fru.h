@@ -149,24 +149,21 @@ int gw_profile_read(gw_ctx *ctx, double *stage_kernel_ms, unsigned long long *st
 int gw_launches(gw_ctx *ctx, unsigned long long *count);
 int gw_l2_flush(gw_ctx *ctx);
 int gw_probe_fp64_peak(double *tflops);
-/* Microseconds per evaluation of the global right-hand side (fcn.c) on one
- * GPU thread and on the host: what a device-resident integrator would pay
- * per stage on GB300's FP64 rate. */
-int gw_probe_fcn(double *device_us, double *host_us);
-/* exp() of n arguments as the device evaluates it and with the host libm:
- * exp is the FRU path's only transcendental, and the two may round
- * differently in the last place. */
-int gw_probe_exp(const double *x, double *device_y, double *host_y, int n);
 
 /* Allocation-free FRU stage (no counterpart in the reference).  For callers
  * that cannot allocate device memory while they run -- cudaMalloc
  * synchronises the device, is not allowed during stream capture, and is off
  * limits to hosts that own all device memory -- this advances FRU arrays the
- * caller owns on the device over [t0, tf] exactly as gw_stage does and writes
+ * caller owns on the device over [t0, tf] with the plain FP64 method (the
+ * one-thread-per-FRU kernel, the reference PCa, no packed launches: the
+ * results of gw_stage on a context with default settings) and writes
  * out[0..4] = flux sums, out[5..8] = Jxfer, Jtr, ICa, Ito2, out[9] = error
- * flag (a device or host-mapped array of 10 doubles).  Arrays use the device
- * layout of gw_stage: frus[5][stride] f64, chan[4][stride] packed channel
- * words (LCC, VDI, RyR0..4, ClCh nibbles), mti[stride], mt[nfru][640] words.
+ * flag (a device or host-mapped array of 10 doubles): 1 when the substep
+ * limit was reached, 2 when an FRU's mti was outside 0..624 or a channel
+ * state outside its range (LCC 1..12, VDI 1..2, RyR 1..8, ClCh 1..2); such an
+ * FRU is left unchanged.  Arrays use the device layout of gw_stage:
+ * frus[5][stride] f64, chan[4][stride] packed channel words (LCC, VDI,
+ * RyR0..4, ClCh nibbles), mti[stride], mt[nfru][640] words.
  * Its reduction scratch is a fixed array inside the library (about 80 KB per
  * GPU, held until the process exits), which limits nfru to 65,536; larger
  * cells get GW_EINVAL.  No save/resume snapshot is taken on this path.  The

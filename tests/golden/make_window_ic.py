@@ -1,7 +1,7 @@
 """Initial-condition files for the reference arm of bench.py: the 12,500-FRU
-bench cell (rest state, 1 Hz pacing, FRU j seeded 5489 + j) at t = 30, 80,
-130 and 180 ms -- four phases of the bench's timed window [30, 230) ms -- in
-the reference's IC format (initialize_state.c:43-163).
+bench cell (rest state, 1 Hz pacing, FRU j seeded 5489 + j) at t = 30, 50,
+70, ..., 210 ms -- ten evenly spaced phases of the bench's timed window
+[30, 230) ms -- in the reference's IC format (initialize_state.c:43-163).
 
 The trajectory comes from the C host driver over the CPU restatement of the
 FRU path (the composition that reproduces the reference program bit for bit,
@@ -9,7 +9,7 @@ tests/test_host_driver.py); the reference program itself cannot write these
 files because its restart_data closes the r_states file twice
 (data_io.c:220, :265) and aborts before writing the channel states.  The
 reference reads IC files 1250 FRUs at a time (rewinding for larger cells), so
-only the first 1250 FRUs are kept.  Takes about 10 CPU-minutes."""
+only the first 1250 FRUs are kept.  Takes about 15 CPU-minutes."""
 import os
 import shutil
 import subprocess
@@ -20,7 +20,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 from test_host_driver import cpu_driver  # noqa: E402
 
-PHASES = {2: 30, 7: 80, 12: 130, 17: 180}   # checkpoint number -> time (ms), Ndump = 10
+# checkpoint number -> time (ms); with Ndump = 10 checkpoint k is written at (k + 1) * 10 ms
+PHASES = {t // 10 - 1: t for t in range(30, 230, 20)}
 KEEP = 1250
 NAMES = {"r_states": "ic_states_stable.txt", "r_FRU": "ic_FRU_stable.txt", "r_LCh": "ic_LCh_stable.txt",
          "r_RyR": "ic_RyR_stable.txt", "r_Ito2": "ic_Ito2_stable.txt"}
@@ -29,8 +30,9 @@ LINES_PER_FRU = {"r_FRU": 1, "r_LCh": 4, "r_RyR": 4, "r_Ito2": 4}
 
 def main():
     exe = cpu_driver()
+    shutil.rmtree(os.path.join(HERE, "ic_window"), ignore_errors=True)
     with tempfile.TemporaryDirectory() as tmp:
-        subprocess.run([exe, "NFRU_sim=12500", "time_end=181", "ic_file_flag=0", "seed_scheme=0", "seed_base=5489",
+        subprocess.run([exe, "NFRU_sim=12500", "time_end=%d" % (max(PHASES.values()) + 1), "ic_file_flag=0", "seed_scheme=0", "seed_base=5489",
                         "Ndump=10"], cwd=tmp, check=True, stdout=subprocess.DEVNULL)
         for num, t in PHASES.items():
             out = os.path.join(HERE, "ic_window", "t%d" % t)

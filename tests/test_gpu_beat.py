@@ -1,7 +1,10 @@
 """First-beat parity (the FP64 criterion): over the first 1000 ms at NFRU=250
 the GPU path and the reference program consume identical MT19937 draw
 sequences and end in identical channel states for at least 99% of FRUs, and
-the global traces agree."""
+the global traces agree.  Every launch shape the FP64 path ships is run:
+one thread per FRU, four lanes per FRU (8 FRUs per warp), and the packed
+launches the autotuner picks for the FP64 ensemble (4-lane groups taking
+FRUs from a queue, 64 FRUs per warp on average)."""
 import zlib
 
 import numpy as np
@@ -12,10 +15,17 @@ from conftest import golden
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("lanes", [1, 4])
-def test_first_beat_transition_sequences(gw, lanes):
+# (lanes per FRU, packed FRUs per warp; 0 = the fixed layout)
+SHAPES = {"1_lane": (1, 0), "4_lanes": (4, 0), "packed_64_fru_per_warp": (4, 64)}
+
+
+@pytest.mark.parametrize("shape", sorted(SHAPES))
+def test_first_beat_transition_sequences(gw, shape):
+    lanes, per_warp = SHAPES[shape]
     g = golden("beat250.npz")
     cell = gw.Cell(250, fru_lanes=lanes)
+    if per_warp:
+        cell.set_stage_packing((250 + per_warp - 1) // per_warp)
     st = gw.settings()
     state = cell.init_rest(st, scheme=gw.SEED_BASE, base=5489)
     _, states, other, _ = cell.run(state, 0.0, 1000, set_=st, want=("states", "other"))

@@ -1,6 +1,6 @@
 """Ensemble parity over 64 seeds (the reference's serial program vs the GPU
-path, NFRU=250, first beat at 1 Hz) and the mixed-precision check against
-the FP64 GPU run with the same seeds.
+path, NFRU=250 and 1,250, first beat at 1 Hz) and the mixed-precision check
+against the FP64 GPU run with the same seeds.
 
 FP64 vs the reference (stated tolerances): per-ms ensemble means of V within
 0.01 mV, of Cai within 1e-5 of its range, of JSR Ca within 1e-5 relative, of
@@ -92,3 +92,40 @@ def test_mixed_precision_ensemble_vs_fp64(gw, fp64_run):
                                                int(np.sum(np.abs(d_apd) < 0.01))))
     assert pk_rel < 0.01
     assert apd_rel < apd_tol
+
+
+def test_ensemble_matches_reference_1250(gw):
+    """The same first-beat ensemble at 1,250 FRUs, the largest size at which
+    the reference program's 64-seed ensemble is affordable on host cores
+    (tests/golden/ensemble1250.npz), run with the per-stream driver (one host
+    integrator thread and CUDA stream per cell).  With five times the FRUs a
+    last-place difference of the device exp flips a transition in more seeds,
+    after which those seeds follow other (equally valid) stochastic paths, so
+    the criterion is statistical: at every ms the ensemble means of V and Cai
+    lie within 5 standard errors of the reference ensemble's (its per-ms
+    standard deviation / sqrt(64)) plus 0.01 mV / 1e-5 of the Cai range; the
+    mean APD90 and mean peak Cai within 3 standard errors of the paired
+    per-seed differences (or 0.5%)."""
+    g = golden("ensemble1250.npz")
+    nseed, nfru = int(g["nseed"][0]), int(g["nfru"][0])
+    tr, ot = run_ensemble(gw, "fp64", nseed, nfru, 1000, lockstep=False)
+    s = summary(tr, ot)
+    se = 1.0 / np.sqrt(nseed)
+    dv = np.abs(s["V_mean"] - g["V_mean"])
+    v_tol = 5.0 * g["V_std"] * se + 0.01
+    rng = g["Cai_mean"].max() - g["Cai_mean"].min()
+    dc = np.abs(s["Cai_mean"] - g["Cai_mean"])
+    c_tol = 5.0 * g["Cai_std"] * se + 1e-5 * rng
+    d_apd = s["apd90"] - g["apd90"]
+    d_pk = s["peak_Cai"] - g["peak_Cai"]
+    apd_tol = max(0.005 * g["apd90"].mean(), 3.0 * d_apd.std(ddof=1) * se)
+    pk_tol = max(0.005 * g["peak_Cai"].mean(), 3.0 * d_pk.std(ddof=1) * se)
+    same = int(np.sum(np.abs(d_apd) < 0.01))
+    print("ensemble 1250 vs reference: |dV_mean| max %.3g mV (worst ratio to tolerance %.2f), |dCai_mean| max "
+          "%.3g of range (ratio %.2f), APD90 mean %+.3f ms (tol %.3f), peak Cai mean %+.3g (tol %.3g), seeds with "
+          "identical APD90 %d/%d" % (dv.max(), np.max(dv / v_tol), dc.max() / rng, np.max(dc / c_tol),
+                                     d_apd.mean(), apd_tol, d_pk.mean(), pk_tol, same, nseed))
+    assert np.all(dv <= v_tol)
+    assert np.all(dc <= c_tol)
+    assert abs(d_apd.mean()) <= apd_tol
+    assert abs(d_pk.mean()) <= pk_tol

@@ -117,3 +117,37 @@ def test_noalloc_stage_matches_gw_stage(gw):
         for key in ("ltype", "ryr", "ito2", "mti", "mt"):
             np.testing.assert_array_equal(got[key], st_w[key], err_msg="call %d %s" % (k, key))
         np.testing.assert_allclose(got["frus"], st_w["frus"], rtol=RTOL, atol=0)
+
+
+@pytest.mark.gpu
+def test_noalloc_flags_out_of_range_fru_state(gw):
+    """The caller's arrays bypass gw_upload's checks, so the kernel checks
+    each FRU before it reads the MT row or the rate tables: an FRU whose mti
+    or channel state is out of range is left unchanged and out[9] reads 2."""
+    torch = pytest.importorskip("torch")
+    n, stride = 64, 64
+    s = O.rest_set(n, "base", 77)
+    s["mti"][5] = 700            # past the 624-word MT row
+    s["ltype"][9, 2, 0] = 0      # no LCC state 0
+    f = _bind(gw.load())
+    dev = torch.device("cuda:0")
+    frus, chan, mti, mt = _pack(s, stride)
+    t_frus = torch.from_numpy(frus).to(dev)
+    t_chan = torch.from_numpy(chan.view(np.int32)).to(dev)
+    t_mti = torch.from_numpy(mti).to(dev)
+    t_mt = torch.from_numpy(mt.view(np.int32)).to(dev)
+    t_out = torch.zeros(10, dtype=torch.float64, device=dev)
+    d0, df = [-80.0, 1e-4, 0.7], [-79.0, 1e-4, 0.7]
+    rc = f(n, stride, t_frus.data_ptr(), t_chan.data_ptr(), t_mti.data_ptr(), t_mt.data_ptr(), 0.0, 0.1,
+           (C.c_double * 3)(*d0), (C.c_double * 3)(*df), 12500.0 / n, t_out.data_ptr(),
+           C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, gw.load().gw_last_error()
+    torch.cuda.synchronize()
+    assert t_out[9].item() == 2.0
+    got = _unpack(t_frus.cpu().numpy(), t_chan.cpu().numpy().view(np.uint32), t_mti.cpu().numpy(),
+                  t_mt.cpu().numpy().view(np.uint32), n)
+    for bad in (5, 9):
+        np.testing.assert_array_equal(got["mt"][bad], s["mt"][bad])
+        assert got["mti"][bad] == s["mti"][bad]
+        np.testing.assert_array_equal(got["frus"][bad], s["frus"][bad])
+    assert np.any(got["mti"] != s["mti"])  # the valid FRUs advanced
