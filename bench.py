@@ -127,7 +127,10 @@ def parse():
     ap.add_argument("--batch-mode", default="streams", choices=["streams", "lockstep"],
                     help="streams: each cell on its own stream; lockstep: shared batched launches")
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--no-devdp", action="store_true", help="skip the device-integrator batched run")
+    ap.add_argument("--no-devdp", action="store_true", help="skip the device-integrator batched runs")
+    ap.add_argument("--runner", default="streams", choices=["streams", "persistent"],
+                    help="ensemble runner: per-cell host integrators on CUDA streams, or the persistent multi-cell "
+                         "kernel (integrators on the device)")
     ap.add_argument("--precision-ensemble", type=int, nargs=2, metavar=("SEEDS", "MS"), default=None,
                     help="only run the mixed-vs-FP64 ensemble check: SEEDS 12,500-FRU cells per precision "
                          "over [0, MS) ms, APD90 / peak Cai / JSR depletion / open probabilities")
@@ -138,10 +141,12 @@ def parse():
     ap.add_argument("--packed", type=int, default=0,
                     help="force packed launches with 1/N as many warps as 8-FRU groups (no autotuning)")
     ap.add_argument("--tune-ms", type=float, default=2.0, help="simulated window per autotuner candidate")
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[1.0, 10.0, 50.0, 200.0])
-    ap.add_argument("--serve-requests", type=int, default=48,
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[50.0],
+                    help="Poisson arrival rates (req/s) of the serving sweep")
+    ap.add_argument("--serve-requests", type=int, default=16,
                     help="requests per rate (at most rate x 24 s of arrivals, at least 16)")
-    ap.add_argument("--serve-ms", type=float, default=20.0)
+    ap.add_argument("--serve-ms", type=float, default=0.0,
+                    help="cap on each request's simulated ms (0: the full protocol, 1-10 beats or the 200-ms step)")
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--fru-lanes", type=int, default=4, choices=[1, 4],
@@ -499,15 +504,23 @@ def time_ensemble(G, args, dist, precision, clocks=None, traces=False, e2e=False
     n = len(cells)
     t = np.zeros(n)
     old = np.full(n, 0.1)
+    persistent = args.runner == "persistent"
     runner = G.Batch(precision)
+
+    def advance(ms, want):
+        if persistent:
+            r = G.run_persistent(cells, sets, t, states, old, ms, traces=want)
+            return r[:2] if want else None
+        return runner.run(cells, sets, t, states, old, ms, traces=want, lockstep=False)
+
     step = int(args.step_ms)
-    tr = runner.run(cells, sets, t, states, old, int(WINDOW_START_MS), traces=traces, lockstep=False)
+    tr = advance(int(WINDOW_START_MS), traces)
     st_parts, ot_parts = ([tr[0]], [tr[1]]) if traces else ([], [])
     snap = snapshot(cells, t, states, old)
     for _ in range(args.warmup):
-        runner.run(cells, sets, t, states, old, step, lockstep=False)
+        advance(step, False)
     restore(cells, snap, t, states, old)
-    tuning = choose_shape(G, args, cells, sets, t, states, old)
+    tuning = None if persistent else choose_shape(G, args, cells, sets, t, states, old)
     sub0 = sum(c.substeps() for c in cells)
     launch0 = sum(c.launches() for c in cells)
     timer = G.GroupTimer(cells)
@@ -519,9 +532,14 @@ def time_ensemble(G, args, dist, precision, clocks=None, traces=False, e2e=False
         clocks.start()
     for _ in range(args.steps):
         cells[0].l2_flush()
-        timer.start()
-        tr = runner.run(cells, sets, t, states, old, step, traces=traces, lockstep=False)
-        total_ms += timer.stop()
+        if persistent:  # synchronous: one graph launch per step on the library's own stream
+            t0 = time.perf_counter()
+            tr = advance(step, traces)
+            total_ms += (time.perf_counter() - t0) * 1e3
+        else:
+            timer.start()
+            tr = advance(step, traces)
+            total_ms += timer.stop()
         if traces:
             st_parts.append(tr[0])
             ot_parts.append(tr[1])
@@ -529,20 +547,20 @@ def time_ensemble(G, args, dist, precision, clocks=None, traces=False, e2e=False
     dist.barrier()
     out = {"device_ms": dist.max(total_ms), "substeps": sum(c.substeps() for c in cells) - sub0,
            "launches": sum(c.launches() for c in cells) - launch0, "clocks": clk, "tuning": tuning, "cells": n,
-           "window": window_str(args)}
+           "window": window_str(args), "runner": args.runner}
     out["value"] = dist.sum(n * args.steps * args.step_ms) / (out["device_ms"] / 1000.0)
     if traces:
         out["state_trace"] = np.concatenate(st_parts, axis=1)
         out["other_trace"] = np.concatenate(ot_parts, axis=1)
     if e2e:
-        out["e2e"] = time_e2e_steps(args, dist, cells, sets, runner, snap, t, states, old)
+        out["e2e"] = time_e2e_steps(args, dist, cells, sets, advance, snap, t, states, old)
     for c in cells:
         c.close()
     runner.close()
     return out
 
 
-def time_e2e_steps(args, dist, cells, sets, runner, snap, t, states, old):
+def time_e2e_steps(args, dist, cells, sets, advance, snap, t, states, old):
     """The ensemble's timed window through the C-ABI with host buffers, on the
     same (warm) cells put back to the window start: every step uploads each
     cell's full FRU + RNG state and global state from host memory, runs the
@@ -550,8 +568,7 @@ def time_e2e_steps(args, dist, cells, sets, runner, snap, t, states, old):
     import numpy as np
     restore(cells, snap, t, states, old)
     host = [dict(h) for h in snap[0]]
-    h_states = snap[2].copy()
-    h2d = sum(v.nbytes for h in host for v in h.values()) + h_states.nbytes
+    h2d = sum(v.nbytes for h in host for v in h.values()) + states.nbytes
     n = len(cells)
     step = int(args.step_ms)
     dist.barrier()
@@ -561,7 +578,7 @@ def time_e2e_steps(args, dist, cells, sets, runner, snap, t, states, old):
         t0 = time.perf_counter()
         for c, h in zip(cells, host):
             c.upload(h)
-        st_tr, ot_tr = runner.run(cells, sets, t, h_states, old, step, traces=True, lockstep=False)
+        st_tr, ot_tr = advance(step, True)
         host = [c.download() for c in cells]
         e2e_s += time.perf_counter() - t0
         d2h = sum(v.nbytes for h in host for v in h.values()) + st_tr.nbytes + ot_tr.nbytes
@@ -648,6 +665,32 @@ def time_batched_device(G, args, dist):
             "timing": "host wall clock around one graph launch (the run is one CUDA graph)"}
 
 
+def time_batched_persistent(G, args, dist):
+    """The batched workload with the persistent multi-cell kernel
+    (gw_run_persistent): every cell's FRU stages, reductions and integrator
+    steps inside one resident launch."""
+    import numpy as np
+    sizes, cells, sets, states = batch_cells(G, args, dist)
+    n = len(cells)
+    t = np.zeros(n)
+    old = np.full(n, 0.1)
+    G.run_persistent(cells, sets, t, states, old, args.batch_warmup_ms)
+    sub0 = sum(c.substeps() for c in cells)
+    dist.barrier()
+    t0 = time.perf_counter()
+    G.run_persistent(cells, sets, t, states, old, args.batch_ms)
+    wall = time.perf_counter() - t0
+    substeps = sum(c.substeps() for c in cells) - sub0
+    eq_ms = float(np.sum(sizes)) / NFRU * args.batch_ms
+    for c in cells:
+        c.close()
+    return {"value": dist.sum(n * args.batch_ms) / dist.max(wall), "unit": "cell-ms/s (cells of mixed NFRU)",
+            "value_12500_equiv": dist.sum(eq_ms) / dist.max(wall), "cells": n,
+            "window_ms": [args.batch_warmup_ms, args.batch_warmup_ms + args.batch_ms],
+            "fru_substeps_per_s": substeps / wall, "precision": "mixed",
+            "timing": "host wall clock around one persistent launch (the run is one CUDA graph)"}
+
+
 def time_batched(G, args, dist):
     """Many cells at once (per-stream or lockstep gw_batch), one host
     integrator thread per cell; the workload of batch_cells."""
@@ -687,32 +730,49 @@ def time_batched(G, args, dist):
             "timing": "host wall clock around the batched run (one host thread per cell)"}
 
 
-def time_serving(G, args, rate):
-    """Poisson arrivals at `rate` requests/s: NFRU from {1250, 2500, 5000,
-    12500}; half paced (cycle length U(400, 2000) ms), half voltage clamp
-    (hold -100 mV, step to U(-40, 40) mV for 200 ms at 5 ms); each request
-    simulates args.serve_ms from rest (a bounded sample of the full protocols),
-    mixed precision, admitted by device bytes."""
+def serve_requests(G, args, rate):
+    """The request stream of the serving workload: NFRU from {1250, 2500, 5000,
+    12500}; half paced (cycle length U(400, 2000) ms for 1-10 beats, the
+    stimulus 10 ms into each cycle), half voltage clamp (hold -100 mV, step
+    to U(-40, 40) mV from 5 to 205 ms, back to -100 mV until 210 ms); each
+    request simulates its whole protocol from rest (--serve-ms caps it)."""
     import numpy as np
     rng = np.random.default_rng(int(rate * 1000) + 7)
-    n = max(16, min(args.serve_requests, int(rate * 24)))
-    srv = G.Server("mixed", slots=args.serve_slots, mem_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
-                   lockstep=args.batch_mode == "lockstep")
+    n = args.serve_requests
     reqs = []
-    gaps = rng.exponential(1.0 / rate, n)
     for i in range(n):
         r = G.Request()
         r.nfru = int(rng.choice([1250, 2500, 5000, 12500]))
         if rng.random() < 0.5:
-            r.set = G.settings(period=float(rng.uniform(400.0, 2000.0)))
+            cl = float(rng.uniform(400.0, 2000.0))
+            beats = int(rng.integers(1, 11))
+            r.set = G.settings(period=cl)
+            dur = float(np.floor(beats * cl))
         else:
             r.set = G.settings(vclamp_flag=1, vclamp_hold=-100.0, vclamp_set=float(rng.uniform(-40.0, 40.0)),
-                               vclamp_duration=200.0, vclamp_shift=5.0, vclamp_period=10000.0)
+                               vclamp_duration=200.0, vclamp_shift=5.0, vclamp_period=100000.0)
+            dur = 210.0
         r.seed_scheme = G.SEED_BASE
         r.seed = SEED + 1000003 * i
         r.pca_scale = 1.0
-        r.duration_ms = float(args.serve_ms)
+        r.duration_ms = min(dur, args.serve_ms) if args.serve_ms > 0 else dur
         reqs.append(r)
+    return reqs, rng.exponential(1.0 / rate, n)
+
+
+def time_serving(G, args, rate):
+    """Poisson arrivals at `rate` requests/s of the serving workload
+    (serve_requests), mixed precision, admitted by device bytes; the
+    request sizes are reserved up front, so no device allocation runs while
+    requests are on the GPU."""
+    import numpy as np
+    reqs, gaps = serve_requests(G, args, rate)
+    n = len(reqs)
+    srv = G.Server("mixed", slots=args.serve_slots, mem_budget_bytes=int(args.serve_budget_gb * (1 << 30)),
+                   lockstep=args.batch_mode == "lockstep")
+    for size in sorted(set(r.nfru for r in reqs)):
+        srv.reserve(size, min(args.serve_slots, sum(1 for r in reqs if r.nfru == size)))
+    allocs0 = srv.stats()["allocs"]
     t0 = time.perf_counter()
     nxt = t0
     for r, g in zip(reqs, gaps):
@@ -723,15 +783,19 @@ def time_serving(G, args, rate):
         srv.submit(r)
     srv.wait()
     wall = time.perf_counter() - t0
+    st = srv.stats()
     srv.close()
     lat = np.array([r.t_done - r.t_submit for r in reqs])
     wait = np.array([r.t_start - r.t_submit for r in reqs])
     ok = all(r.status == 0 for r in reqs)
-    cell_ms = n * args.serve_ms
-    eq = sum(r.nfru for r in reqs) / NFRU * args.serve_ms
+    cell_ms = sum(r.duration_ms for r in reqs)
+    eq = sum(r.nfru * r.duration_ms for r in reqs) / NFRU
     return {"rate_req_per_s": rate, "requests": n, "ok": ok, "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "mean_queue_wait_s": float(wait.mean()),
-            "cell_ms_per_s": cell_ms / wall, "cell_ms_per_s_12500_equiv": eq / wall}
+            "simulated_ms": cell_ms, "wall_s": wall, "cell_ms_per_s": cell_ms / wall,
+            "cell_ms_per_s_12500_equiv": eq / wall,
+            "device_bytes": {"peak_held": st["peak_held"], "budget": int(args.serve_budget_gb * (1 << 30)),
+                             "allocations_while_serving": st["allocs"] - allocs0}}
 
 
 def apd90(t_ms, v):
@@ -879,12 +943,15 @@ def run_gpu(args, dist):
         batched["speedup_12500_equiv_vs_fp64_one_cell"] = batched["value_12500_equiv"] / one["value"]
         if not args.no_devdp:
             batched["device_integrator"] = time_batched_device(G, args, dist)
+            batched["persistent"] = time_batched_persistent(G, args, dist)
+            batched["persistent"]["speedup_vs_per_stream"] = batched["persistent"]["value"] / batched["value"]
     serving = None
     if not args.no_serve and dist.world == 1:
-        serving = {"protocol": "per request: %g ms from rest, NFRU in {1250,2500,5000,12500}, 50/50 pacing "
-                               "(CL U(400,2000) ms) or voltage clamp (-100 -> U(-40,40) mV), mixed precision, "
-                               "%d worker slots, %g GB admission budget" % (args.serve_ms, args.serve_slots,
-                                                                            args.serve_budget_gb),
+        serving = {"protocol": "per request from rest: NFRU in {1250,2500,5000,12500}, 50/50 pacing (CL U(400,2000) "
+                               "ms, 1-10 beats) or voltage clamp (-100 -> U(-40,40) mV for 200 ms, 210 ms in all)%s, "
+                               "mixed precision, %d worker slots, %g GB admission budget, sizes reserved up front"
+                               % (" capped at %g ms" % args.serve_ms if args.serve_ms > 0 else "", args.serve_slots,
+                                  args.serve_budget_gb),
                    "sweep": [time_serving(G, args, r) for r in args.serve_rates]}
         for r in serving["sweep"]:
             r["speedup_12500_equiv_vs_fp64_one_cell"] = r["cell_ms_per_s_12500_equiv"] / one["value"]
@@ -924,7 +991,9 @@ def run_gpu(args, dist):
                        "precision": ("fp64 (FRU path and global ODE)" if args.precision == "fp64" else
                                      "mixed (FRU rates and local Ca ODE fp32; FRU state, clock, flux sums "
                                      "and global ODE fp64)"),
-                       "integrator": "host Dormand-Prince 5(4) per cell, FRU stages on GPU",
+                       "integrator": ("host Dormand-Prince 5(4) per cell, FRU stages on GPU" if args.runner == "streams"
+                                      else "persistent multi-cell kernel: FRU stages, reductions and Dormand-Prince "
+                                           "5(4) steps of every cell inside one launch"),
                        "fru_lanes": args.fru_lanes,
                        "l2": "flushed between timed steps (512 MB write)",
                        "timing": "device time of each step from before the first cell's first launch to after the "

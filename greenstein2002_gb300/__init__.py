@@ -126,7 +126,11 @@ def bind(path):
         "gw_server_create": ([P(vp), C.c_int, C.c_int, C.c_size_t, C.c_int], C.c_int),
         "gw_run_concurrent": ([C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp], C.c_int),
         "gw_run_device": ([C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp], C.c_int),
+        "gw_run_persistent": ([C.c_int, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp], C.c_int),
+        "gw_probe_persist_watchdog": ([vp, P(Settings), C.c_double, P(C.c_int)], C.c_int),
         "gw_server_submit": ([vp, P(Request)], C.c_int),
+        "gw_server_reserve": ([vp, C.c_int, C.c_int], C.c_int),
+        "gw_server_stats": ([vp, P(C.c_size_t), P(C.c_size_t), P(C.c_ulonglong), P(C.c_ulonglong)], C.c_int),
         "gw_server_wait": ([vp], C.c_int),
         "gw_server_destroy": ([vp], C.c_int),
         "gw_event_record": ([vp, C.c_int], C.c_int),
@@ -139,6 +143,7 @@ def bind(path):
         "gw_probe_fcn": ([P(C.c_double), P(C.c_double)], C.c_int),
         "gw_probe_exp": ([_dp, _dp, _dp, C.c_int], C.c_int),
         "gw_probe_fp64_issue": ([_dp], C.c_int),
+        "gw_probe_div": ([C.c_ulonglong, C.c_longlong, P(C.c_ulonglong)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name, None)
@@ -371,6 +376,15 @@ def fp64_issue_cycles(lib=None):
     return dict(zip(PROBE_ISSUE_CASES, out.tolist()))
 
 
+def div_mismatches(n, seed=1, lib=None):
+    """Quotients of the integer-pipe FP64 division that differ from the
+    hardware division's, over n device-drawn operand pairs (gw_probe_div)."""
+    L = lib if lib is not None else load()
+    m = C.c_ulonglong(0)
+    _check(L.gw_probe_div(int(seed), int(n), C.byref(m)), "gw_probe_div", L)
+    return m.value
+
+
 def fp64_peak_tflops():
     """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
     v = C.c_double(0.0)
@@ -450,6 +464,17 @@ class Server:
     def wait(self):
         _check(self._L.gw_server_wait(self._h), "gw_server_wait", self._L)
 
+    def reserve(self, nfru, count):
+        """Pre-create idle contexts so requests of that size allocate nothing while others run."""
+        _check(self._L.gw_server_reserve(self._h, int(nfru), int(count)), "gw_server_reserve", self._L)
+
+    def stats(self):
+        """{held, peak_held, allocs, frees}: device bytes of contexts held, and allocation counts."""
+        h, p, a, f = C.c_size_t(0), C.c_size_t(0), C.c_ulonglong(0), C.c_ulonglong(0)
+        _check(self._L.gw_server_stats(self._h, C.byref(h), C.byref(p), C.byref(a), C.byref(f)), "gw_server_stats",
+               self._L)
+        return {"held": h.value, "peak_held": p.value, "allocs": a.value, "frees": f.value}
+
     def close(self):
         if self._h:
             self._L.gw_server_destroy(self._h)
@@ -485,11 +510,13 @@ class GroupTimer:
         return ms.value
 
 
-def run_device(cells, sets, t, states, oldsteps, n_steps, traces=False, lib=None):
+def run_device(cells, sets, t, states, oldsteps, n_steps, traces=False, lib=None, persistent=False):
     """Advance the cells n_steps output steps with the device-resident
-    integrator (gw_run_device); t, states (n, 37) and oldsteps advance in
-    place.  With traces=True returns (states (n, n_steps, 37), otherstates
-    (n, n_steps, 12), currents (n, n_steps, 24))."""
+    integrator: the graph of lockstep rounds (gw_run_device) or, with
+    persistent=True, the persistent multi-cell kernel (gw_run_persistent);
+    t, states (n, 37) and oldsteps advance in place.  With traces=True
+    returns (states (n, n_steps, 37), otherstates (n, n_steps, 12),
+    currents (n, n_steps, 24))."""
     L = lib if lib is not None else cells[0]._L
     n = len(cells)
     for a in (t, states, oldsteps):
@@ -499,10 +526,26 @@ def run_device(cells, sets, t, states, oldsteps, n_steps, traces=False, lib=None
     st_tr = np.zeros((n, n_steps, NSTATE)) if traces else None
     ot_tr = np.zeros((n, n_steps, NOTHER)) if traces else None
     cu_tr = np.zeros((n, n_steps, NCUR)) if traces else None
-    _check(L.gw_run_device(n, C.cast(handles, C.c_void_p), C.cast(setarr, C.c_void_p), t.ctypes.data_as(C.c_void_p),
-                           states.ctypes.data_as(C.c_void_p), oldsteps.ctypes.data_as(C.c_void_p), int(n_steps),
-                           _ptr(st_tr), _ptr(ot_tr), _ptr(cu_tr)), "gw_run_device", L)
+    fn, name = (L.gw_run_persistent, "gw_run_persistent") if persistent else (L.gw_run_device, "gw_run_device")
+    _check(fn(n, C.cast(handles, C.c_void_p), C.cast(setarr, C.c_void_p), t.ctypes.data_as(C.c_void_p),
+              states.ctypes.data_as(C.c_void_p), oldsteps.ctypes.data_as(C.c_void_p), int(n_steps),
+              _ptr(st_tr), _ptr(ot_tr), _ptr(cu_tr)), name, L)
     return (st_tr, ot_tr, cu_tr) if traces else None
+
+
+def run_persistent(cells, sets, t, states, oldsteps, n_steps, traces=False, lib=None):
+    """run_device with the persistent multi-cell kernel (gw_run_persistent)."""
+    return run_device(cells, sets, t, states, oldsteps, n_steps, traces=traces, lib=lib, persistent=True)
+
+
+def persist_watchdog(cell, set_, wait_s):
+    """Status of a persistent launch whose cell's next operation is held by a
+    flag that nothing sets (gw_probe_persist_watchdog): 3 when every warp gave
+    up after wait_s seconds without progress and the launch returned."""
+    st = C.c_int(-1)
+    _check(cell._L.gw_probe_persist_watchdog(cell._h, C.byref(set_), float(wait_s), C.byref(st)),
+           "gw_probe_persist_watchdog", cell._L)
+    return st.value
 
 
 # (lanes per FRU, warps per block), or (4, -2) / (4, -4) / (4, -8): packed

@@ -32,6 +32,7 @@ CUDA_UNITS = {
     "gw_noalloc.cu": ["-fmad=false"],
     "gw_tune.cu": [],
     "gw_devdp.cu": ["-fmad=false"],
+    "gw_persist.cu": ["-fmad=false"],
 }
 C_UNITS = ["gw_dp.c", "gw_dropin.c"]
 

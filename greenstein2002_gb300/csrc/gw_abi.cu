@@ -577,6 +577,12 @@ extern "C" int gw_probe_fp64_issue(double* cycles) {
   return GW_OK;
 }
 
+extern "C" int gw_probe_div(unsigned long long seed, long long n, unsigned long long* mismatches) {
+  if (!mismatches || n <= 0) return set_err(GW_EINVAL, "gw_probe_div: bad argument");
+  CK(gw::probe_div(seed, n, mismatches));
+  return GW_OK;
+}
+
 extern "C" int gw_probe_fp64_peak(double* tflops) {
   if (!tflops) return set_err(GW_EINVAL, "gw_probe_fp64_peak: null argument");
   int dev = 0, sms = 0;

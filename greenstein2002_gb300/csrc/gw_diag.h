@@ -30,6 +30,20 @@ int gw_probe_exp(const double *x, double *device_y, double *host_y, int n);
  *   [15]     dependent FFMA (FP32), 1 warp */
 #define GW_PROBE_ISSUE_N 16
 int gw_probe_fp64_issue(double cycles[GW_PROBE_ISSUE_N]);
+/* The FRU kernels' FP64 division on the integer pipe (gw_intdiv.h) against
+ * the hardware division, on n operand pairs the device draws from `seed`
+ * (half arbitrary bit patterns, half normal operands of magnitude
+ * 1e-8 .. 1e4); *mismatches counts quotients whose bits differ. */
+int gw_probe_div(unsigned long long seed, long long n, unsigned long long *mismatches);
+/* The persistent kernel's wait limit, exercised without a fault: one cell
+ * (its current FRU state, globals at rest) runs its first operation, after
+ * which a flag that nothing sets keeps its next operation from being posted;
+ * every warp then waits until nothing has progressed for wait_s seconds
+ * (0 < wait_s <= 10), sets the error status and returns.  Returns GW_OK
+ * when the launch ended that way, with *status = 3 (the watchdog status). */
+typedef struct gw_ctx gw_ctx;
+typedef struct gw_settings gw_settings;
+int gw_probe_persist_watchdog(gw_ctx *cell, const gw_settings *set, double wait_s, int *status);
 
 #ifdef __cplusplus
 }

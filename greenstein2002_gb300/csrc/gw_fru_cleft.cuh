@@ -34,6 +34,7 @@
 
 #include "gw_fru_core.cuh"
 #include "gw_fru_model.cuh"
+#include "gw_intdiv.h"
 #include "gw_kernels.h"
 
 namespace gw {
@@ -63,8 +64,14 @@ __device__ __forceinline__ double divc(double x, double d, double r) {
   return fma(fma(-q, d, x), r, q);
 }
 __device__ __forceinline__ float divc(float x, float d, float r) { return x * r; }
-__device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
+// Divisions by variable divisors.  FP64: the correctly rounded quotient
+// computed on the integer pipe (gw_intdiv.h), the same bits as a / b
+// without the ~6 FP64-pipe slots of the hardware sequence.  FP32: rdiv is
+// the fast approximate quotient, qdiv the correctly rounded one.
+__device__ __forceinline__ double rdiv(double a, double b) { return gw_div_rn(a, b); }
 __device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double qdiv(double a, double b) { return gw_div_rn(a, b); }
+__device__ __forceinline__ float qdiv(float a, float b) { return a / b; }
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rexp(float x) { return expf(x); }
 // e = exp(x) and the GHK denominator e - 1.  FP64: the reference's e - 1.
@@ -388,6 +395,7 @@ template <typename R>
 struct LaneStage {
   R dep0[3], span[3], pca_scale, rinterval;
   double t0, tf, interval;
+  float ihi, ilo;  // the interval as a compensated FP32 pair (the mixed-precision clock)
   // per-lane voltage exponential of the rates: alpha, beta, yCa_inf, tau_yCa
   //   lane 0: alphacf*exp(0.012*(V-35))     lane 1: betacf*exp(-0.05*(V-35))
   //   lane 2: 0.4/(1+exp((V+12.5)/5)) + 0.6  lane 3: 60 + 340/(1+exp((V+30)/12))
@@ -407,6 +415,8 @@ __device__ __forceinline__ void lane_stage(const StageParams& p, const Group& g,
   L.tf = p.tf;
   L.interval = p.tf - p.t0;
   L.rinterval = (R)(1.0 / L.interval);
+  L.ihi = (float)L.interval;
+  L.ilo = (float)(L.interval - (double)L.ihi);
   L.isdiv = g.c >= 2;
   L.cA = L.isdiv ? (g.c == 2 ? R(12.5) : R(30.0)) : R(-35.0);
   L.cR = L.isdiv ? (g.c == 2 ? R(1.0 / 5.0) : R(1.0 / 12.0)) : (g.c == 0 ? R(0.012) : R(-0.05));
@@ -447,12 +457,62 @@ struct CaAcc<float> {
   }
 };
 
+// The FRU's clock over [t0, tf] (simfru_local.c:135-146, :161): the step of
+// a substep is dt = min(dt_rate, tf - t), so the last substep lands on tf.
+// FP64: the reference's time_FRU, an FP64 time (t + (tf - t) is exactly tf,
+// as both are close).  Mixed precision: the time since t0 as a compensated
+// FP32 pair (about 48 bits, far finer than any substep of a stage of at most
+// 0.1 ms), the last substep taking exactly the time that remains -- no FP64
+// instruction or conversion in the substep loop.
+template <typename R>
+struct FruClock;
+template <>
+struct FruClock<double> {
+  double t;
+  __device__ __forceinline__ void begin(const LaneStage<double>& L) { t = L.t0; }
+  __device__ __forceinline__ bool running(const LaneStage<double>& L) const { return t < L.tf; }
+  __device__ __forceinline__ double advance(double dtr, const LaneStage<double>& L) {
+    const double dt64 = imin(dtr, L.tf - t);
+    t = t + dt64;
+    return dt64;
+  }
+  __device__ __forceinline__ double frac(const LaneStage<double>& L) const {
+    return frac_of(t, L.t0, L.interval, L.rinterval);
+  }
+};
+template <>
+struct FruClock<float> {
+  float hi, lo;  // time since t0
+  bool fin;      // the FRU has reached tf
+  __device__ __forceinline__ void begin(const LaneStage<float>& L) {
+    hi = 0.0f;
+    lo = 0.0f;
+    fin = !(L.interval > 0.0);
+  }
+  __device__ __forceinline__ bool running(const LaneStage<float>&) const { return !fin; }
+  __device__ __forceinline__ float advance(float dtr, const LaneStage<float>& L) {
+    const float rem = (L.ihi - hi) + (L.ilo - lo);
+    if (!(dtr < rem)) {
+      fin = true;
+      hi = L.ihi;
+      lo = L.ilo;
+      return rem;
+    }
+    const float s = hi + dtr;  // Knuth's two-sum of hi and dtr
+    const float b = s - hi;
+    lo = lo + ((hi - (s - b)) + (dtr - b));
+    hi = s;
+    return dtr;
+  }
+  __device__ __forceinline__ float frac(const LaneStage<float>& L) const { return (hi + lo) * L.rinterval; }
+};
+
 // One FRU's state in the substep loop, as seen by one lane (its cleft):
-// the FP64 Ca state and clock, channel word, MT position, and the values
+// the FRU Ca state and clock, channel word, MT position, and the values
 // carried from one substep to the next.
 template <typename R>
 struct Fru4 {
-  double t;
+  FruClock<R> clk;
   CaAcc<R> jsr, ss;  // CaJSR and this cleft's CaSS
   uint32_t w, nsub;
   int mti, nopen;
@@ -467,7 +527,7 @@ __device__ __forceinline__ void fru_begin(Fru4<R>& F, const LaneStage<R>& L) {
   for (int i = 0; i < 3; i++) F.dep[i] = L.dep0[i];
   F.lopen = lcc_open(F.w) ? R(1) : R(0);
   F.nopen = ryr_open_count(F.w);
-  F.t = L.t0;
+  F.clk.begin(L);
   ghk_terms(F.dep[0], L.pca_scale, F.e2, F.a2j, F.small);
 }
 
@@ -559,7 +619,6 @@ __device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStag
                                           StageCtx& sc) {
   uint32_t& w = F.w;
   int& mti = F.mti;
-  double& t = F.t;
   R* dep = F.dep;
   R &e2 = F.e2, &a2j = F.a2j, &lopen = F.lopen;
   bool& small = F.small;
@@ -584,7 +643,7 @@ __device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStag
       has7 |= (s == 7);
       has34 |= (s == 3 || s == 4);
     }
-    if ((regime <= 1 && has7) || (regime == 2 && (has7 || has34))) p34 = k34 / (k34 + R(k43));
+    if ((regime <= 1 && has7) || (regime == 2 && (has7 || has34))) p34 = qdiv(k34, k34 + R(k43));
   #pragma unroll
     for (int i = 0; i < kRyR; i++) {
       int s = ryr_of(w, i);
@@ -596,7 +655,7 @@ __device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStag
           exw[2] = exw[3];
           exw[3] = exw[4];
           if (s == 7) s = u_below(y, p34) ? 4 : 3;
-          else s = u_below(y, k56 / (k56 + R(k65))) ? 6 : 5;
+          else s = u_below(y, qdiv(k56, k56 + R(k65))) ? 6 : 5;
         }
       } else if (regime == 1) {
         if (s == 7) {
@@ -631,7 +690,7 @@ __device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStag
       T7 = (R(1) - a1) * R(k32) + a1 * R(k45);
     }
     if (need8) {
-      const R a1 = R(k65) / (k56 + R(k65));
+      const R a1 = qdiv(R(k65), k56 + R(k65));
       T8 = a1 * R(k52) + a1 * k54;
     }
   #pragma unroll
@@ -657,15 +716,13 @@ __device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStag
   R dtr = imin(rdiv(R(0.1), mx), R(10.001e-3));
   const R cmax = gmax(g, imax(R(0.e-3), cass));
   if (ilt(R(1.5e-3), cmax)) dtr = imin(dtr, R(5.001e-3));
-  const double dt64 = imin((double)dtr, L.tf - t);
-  const R dt = (R)dt64;
+  const R dt = F.clk.advance(dtr, L);
   // ---- Heun step (simfru_local.c:149-173) ----
   R dJ, dS;
   fcn_fru4(g, cajsr, cass, dep, e2, a2j, small, lopen, nopen, pca_scale, dJ, dS);
   const R k1J = dt * dJ, k1S = dt * dS;
   const R y1J = cajsr + k1J, y1S = cass + k1S;
-  t = t + dt64;
-  const R frac = frac_of(t, L.t0, L.interval, L.rinterval);
+  const R frac = F.clk.frac(L);
   #pragma unroll
   for (int i = 0; i < 3; i++) dep[i] = L.dep0[i] + frac * L.span[i];
   ghk_terms(dep[0], pca_scale, e2, a2j, small);
@@ -682,16 +739,29 @@ __device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStag
     w = set_field(w, 0, choose_dest(r, d, len, dt, bw[0]));
   }
   if (leave_ge(bw[1], dt, R0[1])) w = set_field(w, 4, 3 - vdi_of(w));
+  // The RyRs that leave their state, then one pass per leaving RyR: the
+  // lanes of a warp share the pass (one rate row and destination walk per
+  // pass for every lane that has a RyR left), instead of one divergent body
+  // per RyR index taken whenever any lane's RyR of that index leaves.  Each
+  // RyR's row depends only on its own state and its cleft's constants, so
+  // the order of the passes does not matter.
+  unsigned pend = 0u;
   #pragma unroll
-  for (int i = 0; i < kRyR; i++) {
-    if (leave_gt(bw[2 + i], dt, R0[2 + i])) {
-      const RyrKT<R> k{k12, k23, k34, k54, k25, k56, regime};
-      R r[4];
-      int d[4];
-      const int len = ryr_row(ryr_of(w, i), k, r, d);
-      w = set_field(w, 8 + 4 * i, choose_dest(r, d, len, dt, bw[2 + i]));
-      moved = true;
-    }
+  for (int i = 0; i < kRyR; i++) pend |= leave_gt(bw[2 + i], dt, R0[2 + i]) ? (1u << i) : 0u;
+  moved = pend != 0u;
+  while (pend) {
+    const int i = __ffs(pend) - 1;
+    pend &= pend - 1u;
+    uint32_t y = bw[2];  // the RyR's uniform, by selection (no dynamic register indexing)
+    y = (i == 1) ? bw[3] : y;
+    y = (i == 2) ? bw[4] : y;
+    y = (i == 3) ? bw[5] : y;
+    y = (i == 4) ? bw[6] : y;
+    const RyrKT<R> k{k12, k23, k34, k54, k25, k56, regime};
+    R r[4];
+    int d[4];
+    const int len = ryr_row(ryr_of(w, i), k, r, d);
+    w = set_field(w, 8 + 4 * i, choose_dest(r, d, len, dt, y));
   }
   if (leave_ge(bw[7], dt, R0[7])) w = set_field(w, 28, 3 - cl_of(w));
   lopen = lcc_open(w) ? R(1) : R(0);
@@ -731,7 +801,7 @@ __device__ __forceinline__ void advance4(StageCtx& sc, const Group& g, bool live
     // all 32 lanes stay in the loop until every FRU of the warp is done, so
     // the warp can regenerate MT rows together; a group whose FRU has
     // reached tf (or never had one) idles
-    bool go = live && F.t < L.tf;
+    bool go = live && F.clk.running(L);
     if (go && F.nsub >= (1u << 22)) {
       overflow = true;
       go = false;
@@ -1020,7 +1090,7 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
   sc.my_hold_epoch = s.hold_epoch;
   sc.dirty = false;
   Fru4<R> F;
-  F.t = 0.0;
+  F.clk = {};
   F.jsr.set(0.0);
   F.ss.set(0.0);
   F.w = 0u;
@@ -1101,7 +1171,7 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
   __syncwarp();
   while (true) {
     const bool has = f >= 0;
-    bool go = has && F.t < LS.tf;
+    bool go = has && F.clk.running(LS);
     if (go && F.nsub >= (1u << 22)) {
       overflow = true;
       go = false;
@@ -1116,7 +1186,7 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
     regen_step(sc, lane, g, go, F, S);
     if (go) substep_b(F, S, LS, g, sc);
     // a group whose FRU reached tf stores it and takes the next one
-    if (has && !(go && F.t < LS.tf)) {
+    if (has && !(go && F.clk.running(LS))) {
       finish();
       f = -1;
       const int ff = take();

@@ -10,6 +10,8 @@
 #pragma once
 #include <stdint.h>
 
+#include "gw_intdiv.h"
+
 namespace gw {
 
 constexpr int kClefts = 4;          // parameters.h:30
@@ -56,6 +58,11 @@ constexpr double k_rate = 0.00127215, k_rate2 = 3.4188;
 constexpr double threshCa34to7 = 0.0368369379834969;
 constexpr double threshCa56to8 = 0.00011447933531005;
 constexpr double threshMAX = 2.0, threshMAXCa = 0.0504410547074504;
+
+// a / b for the rate rows: FP64 on the integer pipe (correctly rounded, the
+// bits of a / b), FP32 as is
+__device__ __forceinline__ double fdiv(double a, double b) { return gw_div_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return a / b; }
 
 __device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
 __device__ __forceinline__ double dmax(double a, double b) { return a < b ? b : a; }
@@ -237,11 +244,11 @@ __device__ __forceinline__ int ryr_row(int s, const RyrKT<T>& k, T r[4], int d[4
       r[0] = T(k52) + k.k54 + k.k56; return 4;
     case 6: r[0] = T(k65); r[1] = T(k65); d[1] = 5; return 2;
     case 7: {
-      const T a1 = k.k34 / (T(k43) + k.k34);
+      const T a1 = fdiv(k.k34, T(k43) + k.k34);
       r[1] = (T(1) - a1) * T(k32); d[1] = 2; r[2] = a1 * T(k45); d[2] = 8; r[0] = r[1] + r[2]; return 3;
     }
     case 8: {
-      const T a1 = T(k65) / (k.k56 + T(k65));
+      const T a1 = fdiv(T(k65), k.k56 + T(k65));
       r[1] = a1 * T(k52); d[1] = 2; r[2] = a1 * k.k54; d[2] = (g == 2) ? 7 : 4; r[0] = r[1] + r[2]; return 3;
     }
     default: r[0] = T(0); return 1;

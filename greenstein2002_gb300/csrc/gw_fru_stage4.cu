@@ -28,7 +28,10 @@ cudaError_t launch_stage4_batch(const BatchArgs& a, int nblocks, int warps, cuda
   return cudaGetLastError();
 }
 
-__global__ void __launch_bounds__(32) fru_stage4_packed_kernel(DevState s, StageParams p) {
+// Eleven single-warp blocks per SM: the MT19937 staging (19,968 B per warp)
+// allows eleven, and the register cap (<= 186 per thread) keeps the integer
+// division's temporaries from lowering that to nine.
+__global__ void __launch_bounds__(32, 11) fru_stage4_packed_kernel(DevState s, StageParams p) {
   cleft::stage_body_packed<double>(s, p, s.out);
 }
 

@@ -130,6 +130,8 @@ cudaError_t probe_fcn(double* device_us, double* host_us);
 cudaError_t probe_exp(const double* x, double* device_y, double* host_y, int n);
 // FP64 issue-cost chains on one SM (gw_diag.h, gw_probe_fp64_issue).
 cudaError_t probe_fp64_issue(double* cycles);
+// gw_div_rn against the hardware division on n device-drawn operand pairs.
+cudaError_t probe_div(unsigned long long seed, long long n, unsigned long long* mismatches);
 cudaError_t launch_seed(const DevState& s, int scheme, uint32_t base, cudaStream_t st);
 
 }  // namespace gw

@@ -6,6 +6,7 @@
 #include <chrono>
 
 #include "gw_cell_model.h"
+#include "gw_intdiv.h"
 #include "gw_kernels.h"
 
 namespace gw {
@@ -241,6 +242,52 @@ cudaError_t probe_fp64_issue(double* cycles) {
   }
   if (e == cudaSuccess) issue_dep_ffma<<<1, 32>>>(d, n, 0.999f, 1e-3f);
   take();
+  cudaFree(d);
+  return e;
+}
+
+// gw_div_rn (the integer-pipe division of the FRU kernels) against the
+// hardware division on the device: every thread draws operand pairs from a
+// splitmix64 stream -- arbitrary bit patterns, then normal operands of
+// magnitude 1e-8 .. 1e4 (the FRU substep's range) -- and counts quotients
+// whose bits differ.
+__device__ __forceinline__ uint64_t div_probe_next(uint64_t& st) {
+  uint64_t z = (st += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__global__ void div_probe_kernel(uint64_t seed, long long per_thread, unsigned long long* bad) {
+  const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  uint64_t st = seed ^ (tid * 0xd1342543de82ef95ull);
+  unsigned long long nbad = 0;
+  for (long long i = 0; i < per_thread; i++) {
+    uint64_t a = div_probe_next(st), b = div_probe_next(st);
+    if (i & 1) {
+      const uint64_t ea = 1023 - 27 + div_probe_next(st) % 41, eb = 1023 - 27 + div_probe_next(st) % 41;
+      a = (a & 0x800fffffffffffffull) | (ea << 52);
+      b = (b & 0x800fffffffffffffull) | (eb << 52);
+    }
+    const double x = __longlong_as_double((long long)a), y = __longlong_as_double((long long)b);
+    const double q = x / y, g = gw_div_rn(x, y);
+    const bool same = __double_as_longlong(q) == __double_as_longlong(g) || (q != q && g != g);
+    nbad += same ? 0ull : 1ull;
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
+cudaError_t probe_div(unsigned long long seed, long long n, unsigned long long* mismatches) {
+  const int threads = 256, blocks = 152 * 8;
+  const long long per = (n + (long long)threads * blocks - 1) / ((long long)threads * blocks);
+  unsigned long long* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof *d);
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof *d);
+  if (e == cudaSuccess) {
+    div_probe_kernel<<<blocks, threads>>>(seed, per, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof *d, cudaMemcpyDeviceToHost);
   cudaFree(d);
   return e;
 }

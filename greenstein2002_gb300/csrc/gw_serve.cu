@@ -5,12 +5,17 @@
 // at the next round.
 //
 // Admission is by bytes of device state (FRU arrays, MT19937 rows and their
-// snapshot copies): a request waits in arrival order until its cell fits in
-// the budget next to the running ones.  Device contexts are pooled per FRU
-// count and reused, so no allocation or free (which would synchronise the
-// device) happens while other requests are running, once a size has been
-// seen.  Each request starts from the rest state with its own seeds, so its
-// result is the same alone and in any mix.
+// snapshot copies).  The server holds at most `mem_budget_bytes` of cell
+// contexts at any time, counting running cells and the idle contexts it keeps
+// for reuse alike.  A request waits in arrival order until one of these
+// holds: an idle context of its FRU count is pooled (no allocation); its
+// cell fits in the budget beside every context held (one allocation); or
+// freeing idle contexts of other sizes makes it fit (those are destroyed
+// first).  Allocating or freeing device memory synchronises the device and
+// so stalls the running requests: gw_server_reserve creates contexts up
+// front, so that a workload of known sizes allocates nothing while it runs.
+// Each request starts from the rest state with its own seeds, so its result
+// is the same alone and in any mix.
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <stdint.h>
@@ -49,38 +54,64 @@ struct gw_server {
   std::deque<gw_request*> queue;
   std::vector<std::thread> workers;
   std::map<int, std::vector<gw_ctx*>> pool;  // idle contexts by FRU count
-  std::vector<gw_ctx*> all;
   gw_batch* batch = nullptr;
   int precision = 0;
   int lockstep = 0;  // 1: members share batched launches; 0: each cell on its own stream
-  size_t budget = 0, in_use = 0;
+  size_t budget = 0;
+  size_t held = 0;        // bytes of every context the server holds (running and idle)
+  size_t peak_held = 0;
+  unsigned long long allocs = 0, frees = 0;
   int pending = 0;  // submitted and not finished
   bool stop = false;
   int device = 0;
 };
 
-static gw_ctx* take_ctx(gw_server* s, int nfru, int* rc) {
-  {
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto& v = s->pool[nfru];
-    if (!v.empty()) {
-      gw_ctx* c = v.back();
-      v.pop_back();
-      return c;
+static size_t idle_bytes_except(const gw_server* s, int nfru) {
+  size_t b = 0;
+  for (const auto& kv : s->pool)
+    if (kv.first != nfru) b += kv.second.size() * gw_cell_bytes(kv.first);
+  return b;
+}
+
+// Under the lock: can the request of nfru FRUs start now?  On success either
+// *ctx is a pooled context, or *make is set (allocate one; the bytes are
+// already counted) and `victims` holds idle contexts to destroy first.
+static bool admit(gw_server* s, int nfru, gw_ctx** ctx, bool* make, std::vector<gw_ctx*>& victims) {
+  auto& v = s->pool[nfru];
+  if (!v.empty()) {
+    *ctx = v.back();
+    v.pop_back();
+    return true;
+  }
+  const size_t need = gw_cell_bytes(nfru);
+  if (s->held + need > s->budget) {
+    if (s->held - idle_bytes_except(s, nfru) + need > s->budget) return false;
+    // free idle contexts of other sizes, largest first, until the cell fits
+    while (s->held + need > s->budget) {
+      int big = -1;
+      for (const auto& kv : s->pool)
+        if (kv.first != nfru && !kv.second.empty() && kv.first > big) big = kv.first;
+      gw_ctx* c = s->pool[big].back();
+      s->pool[big].pop_back();
+      s->held -= gw_cell_bytes(big);
+      victims.push_back(c);
     }
   }
+  s->held += need;
+  if (s->held > s->peak_held) s->peak_held = s->held;
+  *make = true;
+  return true;
+}
+
+static gw_ctx* new_ctx(gw_server* s, int nfru, int* rc) {
   gw_ctx* c = nullptr;
   *rc = gw_create(&c, nfru);
   if (*rc) return nullptr;
   gw_set_precision(c, s->precision);
-  std::lock_guard<std::mutex> lk(s->mu);
-  s->all.push_back(c);
   return c;
 }
 
-static void run_request(gw_server* s, gw_request* r) {
-  int rc = 0;
-  gw_ctx* c = take_ctx(s, r->nfru, &rc);
+static void run_request(gw_server* s, gw_request* r, gw_ctx* c, int rc) {
   r->t_start = now_s();
   if (c) {
     double state[37], t = 0.0, oldstep = r->set.step_max;
@@ -99,7 +130,7 @@ static void run_request(gw_server* s, gw_request* r) {
       if (!rc && r->final_state) memcpy(r->final_state, state, sizeof state);
     }
     std::lock_guard<std::mutex> lk(s->mu);
-    s->pool[r->nfru].push_back(c);
+    s->pool[r->nfru].push_back(c);  // stays held, idle, for the next request of its size
   }
   r->t_done = now_s();
   if (rc) snprintf(r->message, sizeof r->message, "%s", gw_last_error());  // per-thread message
@@ -110,25 +141,34 @@ static void worker(gw_server* s) {
   cudaSetDevice(s->device);
   for (;;) {
     gw_request* r = nullptr;
-    size_t need = 0;
+    gw_ctx* ctx = nullptr;
+    bool make = false;
+    std::vector<gw_ctx*> victims;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      // first come, first served: the head waits until its cell fits
+      // first come, first served: the head waits until its cell can be held
       s->cv_work.wait(lk, [&] {
-        return s->stop || (!s->queue.empty() && s->in_use + gw_cell_bytes(s->queue.front()->nfru) <= s->budget);
+        return s->stop || (!s->queue.empty() && admit(s, s->queue.front()->nfru, &ctx, &make, victims));
       });
-      if (s->stop && s->queue.empty()) return;
-      if (s->queue.empty()) continue;
+      if (!ctx && !make) return;  // stopping with an empty queue
       r = s->queue.front();
       s->queue.pop_front();
-      need = gw_cell_bytes(r->nfru);
-      s->in_use += need;
+      s->frees += victims.size();
+      if (make) s->allocs++;
     }
     s->cv_work.notify_all();
-    run_request(s, r);
+    for (gw_ctx* v : victims) gw_destroy(v);
+    int rc = 0;
+    if (make) {
+      ctx = new_ctx(s, r->nfru, &rc);
+      if (!ctx) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->held -= gw_cell_bytes(r->nfru);
+      }
+    }
+    run_request(s, r, ctx, rc);
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      s->in_use -= need;
       s->pending--;
     }
     s->cv_work.notify_all();
@@ -152,6 +192,41 @@ extern "C" int gw_server_create(gw_server** out, int precision, int slots, size_
   s->budget = mem_budget_bytes;
   for (int i = 0; i < slots; i++) s->workers.emplace_back(worker, s);
   *out = s;
+  return GW_OK;
+}
+
+extern "C" int gw_server_reserve(gw_server* s, int nfru, int count) {
+  if (!s || nfru <= 0 || count < 0) return gw_internal_error(GW_EINVAL, "gw_server_reserve: bad argument");
+  for (int i = 0; i < count; i++) {
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      if (s->held + gw_cell_bytes(nfru) > s->budget)
+        return gw_internal_error(GW_EINVAL, "gw_server_reserve: the contexts exceed the memory budget");
+      s->held += gw_cell_bytes(nfru);
+      if (s->held > s->peak_held) s->peak_held = s->held;
+      s->allocs++;
+    }
+    int rc = 0;
+    gw_ctx* c = new_ctx(s, nfru, &rc);
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!c) {
+      s->held -= gw_cell_bytes(nfru);
+      return rc;
+    }
+    s->pool[nfru].push_back(c);
+  }
+  s->cv_work.notify_all();
+  return GW_OK;
+}
+
+extern "C" int gw_server_stats(gw_server* s, size_t* held, size_t* peak_held, unsigned long long* allocs,
+                               unsigned long long* frees) {
+  if (!s) return gw_internal_error(GW_EINVAL, "gw_server_stats: null server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (held) *held = s->held;
+  if (peak_held) *peak_held = s->peak_held;
+  if (allocs) *allocs = s->allocs;
+  if (frees) *frees = s->frees;
   return GW_OK;
 }
 
@@ -188,7 +263,8 @@ extern "C" int gw_server_destroy(gw_server* s) {
   }
   s->cv_work.notify_all();
   for (auto& w : s->workers) w.join();
-  for (gw_ctx* c : s->all) gw_destroy(c);
+  for (auto& kv : s->pool)
+    for (gw_ctx* c : kv.second) gw_destroy(c);
   gw_batch_destroy(s->batch);
   delete s;
   return GW_OK;

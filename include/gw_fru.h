@@ -253,6 +253,18 @@ int gw_run_concurrent(int n, gw_ctx **cells, const gw_settings *sets, double *t,
  * differences from the host C library). */
 int gw_run_device(int n, gw_ctx **cells, const gw_settings *sets, double *t, double *states, double *oldsteps,
                   int n_steps, double *state_trace, double *other_trace, double *cur_trace);
+/* Persistent multi-cell kernel (the level-B seam of rk54pd, rk_pd54m.c:29, and
+ * the stage dispatch of distrib_simFRU, mpi_master.c:369-469, for many cells
+ * at once): n cells advance n_steps output steps each inside one resident
+ * launch, captured with its copy-back as one CUDA graph.  Warps take FRUs,
+ * reduction chunks and integrator steps from whichever cell has work, so no
+ * cell waits for another's slowest FRU and no host thread or round trip sits
+ * inside a step.  Arguments as gw_run_device; cells must share one precision
+ * and not be in a batch.  A cell's results are the same bits alone, in any
+ * mix and under gw_run_device.  If no work anywhere progresses for 2 s the
+ * launch ends with GW_ECUDA instead of waiting on. */
+int gw_run_persistent(int n, gw_ctx **cells, const gw_settings *sets, double *t, double *states, double *oldsteps,
+                      int n_steps, double *state_trace, double *other_trace, double *cur_trace);
 /* Warps per block of the batch's launches (1, 2, 4 or 8; same results). */
 int gw_batch_set_warps(gw_batch *batch, int warps);
 
@@ -293,10 +305,22 @@ typedef struct gw_request {
 typedef struct gw_server gw_server;
 /* Device bytes a cell of nfru FRUs holds (the admission unit). */
 size_t gw_cell_bytes(int nfru);
-/* slots worker threads; requests are admitted in arrival order while their
- * cells fit in mem_budget_bytes next to the running ones.  lockstep = 1 runs
- * the admitted cells through one gw_batch; 0 gives each its own stream. */
+/* slots worker threads; requests are admitted in arrival order.  The server
+ * holds at most mem_budget_bytes of cell contexts (gw_cell_bytes each),
+ * counting the running cells and the idle contexts it pools for reuse: a
+ * request starts when a pooled context of its FRU count is idle, or when a
+ * new one fits beside everything held, destroying idle contexts of other
+ * sizes if that makes it fit.  lockstep = 1 runs the admitted cells through
+ * one gw_batch; 0 gives each its own stream. */
 int gw_server_create(gw_server **srv, int precision, int slots, size_t mem_budget_bytes, int lockstep);
+/* Create `count` idle contexts of nfru FRUs now (within the budget), so that
+ * requests of that size allocate nothing -- no device-wide synchronisation --
+ * while other requests run. */
+int gw_server_reserve(gw_server *srv, int nfru, int count);
+/* Bytes of contexts held now and at most so far, and the context allocations
+ * and frees made so far (reserve included). */
+int gw_server_stats(gw_server *srv, size_t *held, size_t *peak_held, unsigned long long *allocs,
+                    unsigned long long *frees);
 /* Non-blocking; req must stay valid until gw_server_wait returns. */
 int gw_server_submit(gw_server *srv, gw_request *req);
 int gw_server_wait(gw_server *srv);

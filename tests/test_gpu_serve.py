@@ -81,3 +81,35 @@ def test_failed_request_carries_its_message(gw):
     srv.close()
     assert bad.status != 0 and b"scheme 7" in bad.message
     assert good.status == 0 and good.message == b""
+
+
+def test_held_bytes_never_exceed_the_budget(gw):
+    """Pooled idle contexts count against the budget: with room for two
+    1000-FRU cells, requests of another size first free idle contexts, and
+    the bytes held never pass the budget."""
+    budget = 2 * gw.cell_bytes(1000) + 1024
+    srv = gw.Server("mixed", slots=4, mem_budget_bytes=budget)
+    reqs = [_req(gw, 1000, 200 + i, dur=3) for i in range(3)] + [_req(gw, 700, 300 + i, dur=3) for i in range(3)]
+    for r in reqs:
+        srv.submit(r)
+    srv.wait()
+    st = srv.stats()
+    srv.close()
+    assert all(r.status == 0 for r in reqs)
+    assert st["peak_held"] <= budget
+    assert st["frees"] >= 1  # idle 1000-FRU contexts made room for the 700-FRU cells
+
+
+def test_reserved_contexts_allocate_nothing_while_running(gw):
+    srv = gw.Server("mixed", slots=4, mem_budget_bytes=8 << 30)
+    srv.reserve(400, 3)
+    srv.reserve(900, 3)
+    a0 = srv.stats()["allocs"]
+    reqs = [_req(gw, 400, 10 + i, dur=3) for i in range(3)] + [_req(gw, 900, 20 + i, dur=3) for i in range(3)]
+    for r in reqs:
+        srv.submit(r)
+    srv.wait()
+    st = srv.stats()
+    srv.close()
+    assert all(r.status == 0 for r in reqs)
+    assert st["allocs"] == a0 == 6
