@@ -135,6 +135,9 @@ def parse():
                     help="only run the mixed-vs-FP64 ensemble check: SEEDS 12,500-FRU cells per precision "
                          "over [0, MS) ms, APD90 / peak Cai / JSR depletion / open probabilities")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--full-cell", action="store_true",
+                    help="also run the full-size cell's whole protocol through the C host driver: 5 beats at 1 Hz "
+                         "and the -100 -> 0 mV, 200-ms clamp, FP64 and mixed precision")
     ap.add_argument("--only-ensemble", action="store_true",
                     help="run the headline ensemble section alone (for launch lists: its timed launches are the run's "
                          "last `gpu_launches` launches)")
@@ -798,6 +801,64 @@ def time_serving(G, args, rate):
                              "allocations_while_serving": st["allocs"] - allocs0}}
 
 
+def caf_run(settings, workdir):
+    """Run the C host driver (gw_caf, the reference program's main loop over
+    libgw_fru.so) with key=value settings; returns (wall s, states,
+    otherstates, currents) read back from its reference-format files, time
+    in ms."""
+    import numpy as np
+    exe = os.path.join(ROOT, "greenstein2002_gb300", "_build", "gw_caf")
+    os.makedirs(workdir, exist_ok=True)
+    t0 = time.perf_counter()
+    r = subprocess.run([exe] + ["%s=%s" % kv for kv in settings.items()] + ["output_dir=%s/" % workdir],
+                       capture_output=True, text=True)
+    wall = time.perf_counter() - t0
+    if r.returncode != 0:
+        raise RuntimeError("gw_caf failed: %s" % r.stderr[-500:])
+
+    def load(stem):
+        a = np.loadtxt(os.path.join(workdir, "%s.0.txt" % stem), skiprows=1)
+        a[:, 0] *= 1000.0  # the files' time column is in seconds (caf.c's ts_sec)
+        return a
+    return wall, load("states"), load("otherstates"), load("currents")
+
+
+def time_full_cell(args):
+    """The full-size cell's whole protocol, one cell, through the C host
+    driver writing the reference's output files: 5 beats at 1 Hz from rest
+    (stimulus 10 ms into each cycle), and a voltage-clamp run holding -100 mV
+    with a step to 0 mV from 50 to 250 ms (300 ms in all) that records ICaL
+    and the SR release flux.  FP64 (packed launches, 16 FRUs per warp, the
+    one-cell autotuner's choice) and mixed precision with the same seeds."""
+    import tempfile
+    out = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for prec, extra in (("fp64", {"precision": 0, "stage_packing": 2}), ("mixed", {"precision": 1})):
+            base = dict(NFRU_sim=NFRU, ic_file_flag=0, seed_scheme=0, seed_base=SEED, **extra)
+            w1, st, ot, cu = caf_run(dict(base, time_end=5000), os.path.join(tmp, prec + "_pace"))
+            beats = []
+            for b in range(5):
+                sel = (st[:, 0] > 1000 * b) & (st[:, 0] <= 1000 * (b + 1))
+                beats.append({"apd90_ms": apd90(st[sel, 0], st[sel, 1]), "peak_cai_mM": float(st[sel, 7].max()),
+                              "min_cajsr_mM": float(ot[sel, 2].min())})
+            w2, st2, ot2, cu2 = caf_run(dict(base, time_end=300, vclamp_flag=1, vclamp_hold=-100, vclamp_set=0,
+                                             vclamp_duration=200, vclamp_shift=50, vclamp_period=1000),
+                                        os.path.join(tmp, prec + "_clamp"))
+            step = (st2[:, 0] > 50) & (st2[:, 0] <= 250)
+            out[prec] = {"value": 5300.0 / (w1 + w2), "unit": "cell-ms/s", "wall_s": {"pacing": w1, "clamp": w2},
+                         "beats": beats,
+                         "clamp": {"peak_ICaL_uA_per_uF": float(cu2[step, 12].min()),
+                                   "ICaL_at_step_end": float(cu2[step, 12][-1]),
+                                   "peak_JRyRtot": float(ot2[step, 3].max()),
+                                   "peak_cai_mM": float(st2[step, 7].max())}}
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["protocol"] = ("one 12,500-FRU cell (FRU j seeded 5489 + j), rest state: 5 beats at 1 Hz (5000 ms), then a "
+                       "separate clamp run (hold -100 mV, 0 mV from 50 to 250 ms, 300 ms); through gw_caf, which "
+                       "writes the reference program's states/otherstates/currents files; value = 5300 simulated ms / "
+                       "wall s of both runs (host integrator, FRU stages on the GPU)")
+    return out
+
+
 def apd90(t_ms, v):
     """Action-potential duration at 90% repolarisation of the first beat (from
     the upstroke's crossing of the 90% level to the repolarisation's)."""
@@ -956,6 +1017,7 @@ def run_gpu(args, dist):
         for r in serving["sweep"]:
             r["speedup_12500_equiv_vs_fp64_one_cell"] = r["cell_ms_per_s_12500_equiv"] / one["value"]
     e2e = ens.get("e2e")
+    full_cell = time_full_cell(args) if args.full_cell and dist.world == 1 else None
 
     # ---- CPU baseline: the reference program on one host core ----
     cpu = None
@@ -1018,6 +1080,7 @@ def run_gpu(args, dist):
             "mixed": mixed,
             "batched": batched,
             "serving": serving,
+            "full_cell": full_cell,
             "e2e": e2e,
             "cpu_baseline": cpu,
         }
