@@ -143,6 +143,8 @@ def bind(path):
         "gw_probe_fcn": ([P(C.c_double), P(C.c_double)], C.c_int),
         "gw_probe_exp": ([_dp, _dp, _dp, C.c_int], C.c_int),
         "gw_probe_fp64_issue": ([_dp], C.c_int),
+        "gw_probe_fcn_warp": ([P(C.c_double)], C.c_int),
+        "gw_probe_fcn_compare": ([_dp, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp, _dp], C.c_int),
         "gw_probe_div": ([C.c_ulonglong, C.c_longlong, P(C.c_ulonglong)], C.c_int),
     }
     for name, (args, res) in sig.items():
@@ -383,6 +385,27 @@ def div_mismatches(n, seed=1, lib=None):
     m = C.c_ulonglong(0)
     _check(L.gw_probe_div(int(seed), int(n), C.byref(m)), "gw_probe_div", L)
     return m.value
+
+
+def fcn_warp_us(lib=None):
+    """Microseconds per evaluation of the global right-hand side on one warp."""
+    L = lib if lib is not None else load()
+    v = C.c_double(0.0)
+    _check(L.gw_probe_fcn_warp(C.byref(v)), "gw_probe_fcn_warp", L)
+    return v.value
+
+
+def fcn_thread_vs_warp(states, time, clamp=False, lib=None):
+    """(F one thread, F warp, currents one thread, currents warp) of the
+    global right-hand side for states (n, 37) at `time`."""
+    L = lib if lib is not None else load()
+    states = np.ascontiguousarray(states, np.float64)
+    n = states.shape[0]
+    Fs, Fw = np.zeros((n, NSTATE)), np.zeros((n, NSTATE))
+    Cs, Cw = np.zeros((n, NCUR)), np.zeros((n, NCUR))
+    _check(L.gw_probe_fcn_compare(states.reshape(-1), n, float(time), 1 if clamp else 0, Fs.reshape(-1),
+                                  Fw.reshape(-1), Cs.reshape(-1), Cw.reshape(-1)), "gw_probe_fcn_compare", L)
+    return Fs, Fw, Cs, Cw
 
 
 def fp64_peak_tflops():

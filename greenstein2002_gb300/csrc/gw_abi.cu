@@ -583,6 +583,19 @@ extern "C" int gw_probe_div(unsigned long long seed, long long n, unsigned long 
   return GW_OK;
 }
 
+extern "C" int gw_probe_fcn_warp(double* us) {
+  if (!us) return set_err(GW_EINVAL, "gw_probe_fcn_warp: null argument");
+  CK(gw::probe_fcn_warp(us));
+  return GW_OK;
+}
+
+extern "C" int gw_probe_fcn_compare(const double* states, int n, double time, int clamp, double* Fs, double* Fw,
+                                    double* Cs, double* Cw) {
+  if (!states || n <= 0 || !Fs || !Fw || !Cs || !Cw) return set_err(GW_EINVAL, "gw_probe_fcn_compare: bad argument");
+  CK(gw::probe_fcn_compare(states, n, time, clamp, Fs, Fw, Cs, Cw));
+  return GW_OK;
+}
+
 extern "C" int gw_probe_fp64_peak(double* tflops) {
   if (!tflops) return set_err(GW_EINVAL, "gw_probe_fp64_peak: null argument");
   int dev = 0, sms = 0;

@@ -111,59 +111,117 @@ GW_HD double gw_errweight(int i) {
   }
 }
 
-/* Global right-hand side (fcn.c:29-1072).  May overwrite state[GW_mNa]
- * (V < -90 mV steady state) and state[GW_V] (clamp modes) in place, as the
- * reference does.  current[] is filled when keepc != 0. */
-GW_HD void gw_fcn(const double time, double* state, double* F, double* current, const int keepc,
-                  const double Jxfer, const double Jtr, const double ICa, const double Ito2, const gw_protocol* P) {
-  /* membrane current parameters, fcn.c:169-264 */
-  const double GKr = 0.029 * P->scale_GKr, GKs = 0.035, GK1 = 3.0, GKp = 1.2 * 0.002216, GNa = 12.8;
-  const double kNaCa = 0.9 * 0.30, KmNa = 87.5, KmCa = 1.38, KmK1 = 13.0, ksat = 0.2, eta = 0.35;
-  const double INaKmax = 1.3 * 0.693, KmNai = 10.0, KmKo = 1.5, IpCamax = 0.6 * 0.05, KmpCa = 0.0005;
-  const double GCab = 3.3 * 7.684e-5, GNab = 0.001;
-  const double Kfb = 0.26e-3, Krb = 1.8, KSR = 1.0, Nfb = 0.75, Nrb = 0.75;
-  const double vmaxf = 1.53 * 137.0e-6, vmaxr = 1.53 * 137.0e-6;
-  const double KvScale = 1.13 * 1.03 * 1.55, Kv43Frac = 0.77;
-  const double GKv43 = Kv43Frac * KvScale * 0.1;
-  const double PKv14 = (1.0 - Kv43Frac) * KvScale * 4.792933e-7;
-  const double alphaa0Kv43 = 0.543708, aaKv43 = 0.028983, betaa0Kv43 = 0.080185, baKv43 = 0.0468437;
-  const double alphai0Kv43 = 0.0498424, aiKv43 = 0.000373016, betai0Kv43 = 0.000819482, biKv43 = 0.00000005374;
-  const double alphaa0Kv14 = 6.0 * 0.31551, aaKv14 = 0.00695, betaa0Kv14 = 6.0 * 0.001966, baKv14 = 0.08527;
-  const double alphai0Kv14 = 6.0 * 0.0004938, betai0Kv14 = 6.0 * 0.0000176;
-  const double f1Kv43 = 1.8936, f2Kv43 = 14.224647456, f3Kv43 = 158.574378389, f4Kv43 = 142.936645351;
-  const double b1Kv43 = 6.77348, b2Kv43 = 15.6212705152, b3Kv43 = 28.7532603313, b4Kv43 = 524.576206679;
-  const double f1Kv14 = 0.20005, f2Kv14 = 0.320280, f3Kv14 = 13.50909223, f4Kv14 = 1151.7651385;
-  const double b1Kv14 = 2.2300, b2Kv14 = 12.000299, b3Kv14 = 5.3701338025, b4Kv14 = 5.2396395511;
-  const double T_Const_HERG = 5.320000001;
-  const double A0_HERG = 0.017147641733086, B0_HERG = 0.03304608038835;
-  const double A1_HERG = 0.03969328381141, B1_HERG = -0.04306054163980;
-  const double A2_HERG = 0.02057448605977, B2_HERG = 0.02617412715118;
-  const double A3_HERG = 0.00134366604423, B3_HERG = -0.02691385498399;
-  const double A4_HERG = 0.10666316491288, B4_HERG = 0.00568908859717;
-  const double A5_HERG = 0.00646393910049, B5_HERG = -0.04536642959543;
-  const double A6_HERG = 0.00008039374403, B6_HERG = 0.00000069808924;
-  const double C2H_to_C3H = T_Const_HERG * 0.02608362043337;
-  const double C3H_to_C2H = T_Const_HERG * 0.14832978132145;
-  const double RT_over_F = GWC_RT_over_F, Faraday = GWC_Faraday, Ko = GWC_Ko, Nao = GWC_Nao, Cao = GWC_Cao;
-  const double Acap = GWC_Acap, Vmyo = GWC_Vmyo, VNSR = GWC_VNSR, VJSR = GWC_VJSR, VSS = GWC_VSS;
+/* ---- transcendental terms of the right-hand side ------------------------------
+ * Every exp, log and pow of fcn.c:549-998 depends only on the (clamped)
+ * membrane potential and on concentrations, except K1_inf's exp, which
+ * depends on EK (a log).  gw_tx holds them all, so that a GPU warp can
+ * evaluate them side by side -- one per lane, the same function on every
+ * lane -- before the arithmetic that combines them (gw_fcn_tx); each entry
+ * is the value fcn.c computes, from the same operands by the same
+ * operations.  The 34 exponents share one form, ((V or 0) + d) op c [* e]
+ * with op a multiplication or a division: fcn.c's expressions rewritten by
+ * commutation and sign symmetry only (a - b = -(b - a), -x / c = x / -c,
+ * x - d = x + (-d)), which round identically. */
+enum {
+  GW_X_VFRT = 0, GW_X_KPV, GW_X_SIGMA, GW_X_NAK, GW_X_ETA, GW_X_AM, GW_X_BM, GW_X_AH, GW_X_BH1, GW_X_BH2, GW_X_BH3,
+  GW_X_AJ1, GW_X_AJ2, GW_X_AJ3, GW_X_BJ1, GW_X_BJ2, GW_X_BJ3, GW_X_BJ4, GW_X_H0, GW_X_H1, GW_X_H2, GW_X_H3, GW_X_H4,
+  GW_X_H5, GW_X_H6, GW_X_XKS, GW_X_KS1, GW_X_KS2, GW_X_43A, GW_X_43B, GW_X_43C, GW_X_43D, GW_X_14A, GW_X_14B, GW_NX
+};
+enum { GW_XF_V = 1, GW_XF_ADD = 2, GW_XF_DIV = 4, GW_XF_MUL2 = 8 };
+typedef struct gw_tx {
+  double x[GW_NX]; /* exp of the exponents above */
+  double lg[4];    /* log(Nao/Nai), log(Ko/Ki), log(a1/a2) of EKs, log(Cao/Cai) */
+  double pw[6];    /* pow(Ko/4, 0.5), pow(KmNai/Nai, 1.5), fb, rb, (Cai+KmCMDN)^2, (Cai+KmEGTA)^2 */
+  double k1;       /* exp(1.76/RT_over_F (V - EK)) of K1_inf */
+} gw_tx;
 
-  double V, mNa = state[GW_mNa], hNa = state[GW_hNa], jNa = state[GW_jNa], Nai = state[GW_Nai];
-  double Ki = state[GW_Ki], Cai = state[GW_Cai], CaNSR = state[GW_CaNSR], xKs = state[GW_xKs];
-  double LTRPNCa = state[GW_LTRPNCa], HTRPNCa = state[GW_HTRPNCa];
-  const double C0Kv43 = state[GW_C0Kv43], C1Kv43 = state[GW_C1Kv43], C2Kv43 = state[GW_C2Kv43];
-  const double C3Kv43 = state[GW_C3Kv43], OKv43 = state[GW_OKv43], CI0Kv43 = state[GW_CI0Kv43];
-  const double CI1Kv43 = state[GW_CI1Kv43], CI2Kv43 = state[GW_CI2Kv43], CI3Kv43 = state[GW_CI3Kv43];
-  const double OIKv43 = 1.0 - CI0Kv43 - CI1Kv43 - CI2Kv43 - CI3Kv43 - OKv43 - C0Kv43 - C1Kv43 - C2Kv43 - C3Kv43;
-  const double C0Kv14 = state[GW_C0Kv14], C1Kv14 = state[GW_C1Kv14], C2Kv14 = state[GW_C2Kv14];
-  const double C3Kv14 = state[GW_C3Kv14], OKv14 = state[GW_OKv14], CI0Kv14 = state[GW_CI0Kv14];
-  const double CI1Kv14 = state[GW_CI1Kv14], CI2Kv14 = state[GW_CI2Kv14], CI3Kv14 = state[GW_CI3Kv14];
-  const double OIKv14 = 1.0 - CI0Kv14 - CI1Kv14 - CI2Kv14 - CI3Kv14 - OKv14 - C0Kv14 - C1Kv14 - C2Kv14 - C3Kv14;
-  const double C1Herg = state[GW_C1Herg], C2Herg = state[GW_C2Herg], C3Herg = state[GW_C3Herg];
-  const double OHerg = state[GW_OHerg];
-  const double IHerg = 1.0 - OHerg - C1Herg - C2Herg - C3Herg;
-  double Istim, a1, a2, a3, a4, a5;
-  V = state[GW_V];
+/* exponent k: flags, d, c, e (fcn.c:565-998) */
+GW_HD int gw_x_form(int k, double* d, double* c, double* e) {
+  const double RT = GWC_RT_over_F;
+  *d = 0.0;
+  *e = 1.0;
+  switch (k) {
+    case GW_X_VFRT: *c = RT; return GW_XF_V | GW_XF_DIV;                                  /* V/RT */
+    case GW_X_KPV: *d = -7.488; *c = -5.98; return GW_XF_V | GW_XF_ADD | GW_XF_DIV;       /* (7.488 - V)/5.98 */
+    case GW_X_SIGMA: *d = GWC_Nao; *c = 67.3; return GW_XF_ADD | GW_XF_DIV;               /* Nao/67.3 */
+    case GW_X_NAK: *c = RT; *e = -0.1; return GW_XF_V | GW_XF_DIV | GW_XF_MUL2;           /* -0.1 VF/RT */
+    case GW_X_ETA: *c = RT; *e = 0.35; return GW_XF_V | GW_XF_DIV | GW_XF_MUL2;           /* eta VF/RT */
+    case GW_X_AM: *d = 47.13; *c = -0.1; return GW_XF_V | GW_XF_ADD;                      /* -0.1 (V + 47.13) */
+    case GW_X_BM: *c = -11.0; return GW_XF_V | GW_XF_DIV;                                 /* -V/11 */
+    case GW_X_AH: *d = 80.0; *c = -6.8; return GW_XF_V | GW_XF_ADD | GW_XF_DIV;           /* (80 + V)/-6.8 */
+    case GW_X_BH1: *c = 0.079; return GW_XF_V;
+    case GW_X_BH2: *c = 0.35; return GW_XF_V;
+    case GW_X_BH3: *d = 10.66; *c = -11.1; return GW_XF_V | GW_XF_ADD | GW_XF_DIV;
+    case GW_X_AJ1: *c = 0.2444; return GW_XF_V;
+    case GW_X_AJ2: *c = -0.04391; return GW_XF_V;
+    case GW_X_AJ3: *d = 79.23; *c = 0.311; return GW_XF_V | GW_XF_ADD;
+    case GW_X_BJ1: *c = -0.01052; return GW_XF_V;
+    case GW_X_BJ2: *d = 40.14; *c = -0.1378; return GW_XF_V | GW_XF_ADD;
+    case GW_X_BJ3: *c = -2.535E-7; return GW_XF_V;
+    case GW_X_BJ4: *d = 32.0; *c = -0.1; return GW_XF_V | GW_XF_ADD;
+    case GW_X_H0: *c = 0.03304608038835; return GW_XF_V;   /* B0_HERG .. B6_HERG */
+    case GW_X_H1: *c = -0.04306054163980; return GW_XF_V;
+    case GW_X_H2: *c = 0.02617412715118; return GW_XF_V;
+    case GW_X_H3: *c = -0.02691385498399; return GW_XF_V;
+    case GW_X_H4: *c = 0.00568908859717; return GW_XF_V;
+    case GW_X_H5: *c = -0.04536642959543; return GW_XF_V;
+    case GW_X_H6: *c = 0.00000069808924; return GW_XF_V;
+    case GW_X_XKS: *d = -24.7; *c = -13.6; return GW_XF_V | GW_XF_ADD | GW_XF_DIV;        /* -(V - 24.7)/13.6 */
+    case GW_X_KS1: *d = -10.0; *c = -0.148; return GW_XF_V | GW_XF_ADD;
+    case GW_X_KS2: *d = -10.0; *c = 0.0687; return GW_XF_V | GW_XF_ADD;
+    case GW_X_43A: *c = 0.028983; return GW_XF_V;           /* aaKv43, -baKv43, -aiKv43, biKv43 */
+    case GW_X_43B: *c = -0.0468437; return GW_XF_V;
+    case GW_X_43C: *c = -0.000373016; return GW_XF_V;
+    case GW_X_43D: *c = 0.00000005374; return GW_XF_V;
+    case GW_X_14A: *c = 0.00695; return GW_XF_V;            /* aaKv14, -baKv14 */
+    default: *c = -0.08527; return GW_XF_V;                 /* GW_X_14B */
+  }
+}
 
+GW_HD double gw_x_arg(int k, double V) {
+  double d, c, e;
+  const int f = gw_x_form(k, &d, &c, &e);
+  double t = (f & GW_XF_V) ? V : 0.0;
+  if (f & GW_XF_ADD) t = t + d;
+  t = (f & GW_XF_DIV) ? t / c : t * c;
+  if (f & GW_XF_MUL2) t = t * e;
+  return t;
+}
+
+/* Cai as fcn.c:558 uses it from there on */
+GW_HD double gw_cai_clamped(const double* state) { return state[GW_Cai] <= 0.0 ? 1.e-15 : state[GW_Cai]; }
+
+/* argument of log k and base / exponent of pow k */
+GW_HD double gw_lg_arg(int k, const double* state) {
+  const double Nai = state[GW_Nai], Ki = state[GW_Ki];
+  switch (k) {
+    case 0: return GWC_Nao / Nai;
+    case 1: return GWC_Ko / Ki;
+    case 2: return (GWC_Ko + 0.01833 * GWC_Nao) / (Ki + 0.01833 * Nai);
+    default: return GWC_Cao / gw_cai_clamped(state);
+  }
+}
+GW_HD double gw_pw_arg(int k, const double* state, double* y) {
+  const double Cai = gw_cai_clamped(state);
+  switch (k) {
+    case 0: *y = 0.5; return GWC_Ko / 4.0;
+    case 1: *y = 1.5; return 10.0 / state[GW_Nai];            /* KmNai / Nai */
+    case 2: *y = 0.75; return Cai / 0.26e-3;                   /* Cai / Kfb, Nfb */
+    case 3: *y = 0.75; return state[GW_CaNSR] / 1.8;           /* CaNSR / Krb, Nrb */
+    case 4: *y = 2.0; return Cai + GWC_KmCMDN;
+    default: *y = 2.0; return Cai + GWC_KmEGTA;
+  }
+}
+/* exponent of K1_inf's exp: 1.76/RT_over_F (V - EK) */
+GW_HD double gw_k1_arg(double V, const double* tx_lg) {
+  const double EK = GWC_RT_over_F * tx_lg[1];
+  return 1.76 / GWC_RT_over_F * (V - EK);
+}
+
+/* Membrane potential of fcn.c:434-535: the state's V, or the clamp level of
+ * an active clamp protocol; *Istim receives the applied stimulus. */
+GW_HD double gw_fcn_voltage(const double time, const double* state, const gw_protocol* P, double* Istim_out) {
+  double V = state[GW_V], Istim;
   /* ---- applied stimulus, fcn.c:434-443 ---- */
   {
     const double on = floor((time - P->shift) / P->period) * P->period;
@@ -202,25 +260,82 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
     else V = P->iv_clamp_hold;
   }
 
+  *Istim_out = Istim;
+  return V;
+}
+
+/* Global right-hand side (fcn.c:29-1072) given its transcendental terms
+ * (gw_tx, filled for this state and time).  May overwrite state[GW_mNa]
+ * (V < -90 mV steady state) and state[GW_V] (clamp modes) in place, as the
+ * reference does.  current[] is filled when keepc != 0. */
+GW_HD void gw_fcn_tx(const double time, double* state, double* F, double* current, const int keepc,
+                     const double Jxfer, const double Jtr, const double ICa, const double Ito2, const gw_protocol* P,
+                     const gw_tx* tx) {
+  /* membrane current parameters, fcn.c:169-264 */
+  const double GKr = 0.029 * P->scale_GKr, GKs = 0.035, GK1 = 3.0, GKp = 1.2 * 0.002216, GNa = 12.8;
+  /* eta, KmNai, Kfb, Krb, Nfb, Nrb and the exponents' rate constants enter
+   * only the transcendental terms (gw_x_form, gw_pw_arg) */
+  const double kNaCa = 0.9 * 0.30, KmNa = 87.5, KmCa = 1.38, KmK1 = 13.0, ksat = 0.2;
+  const double INaKmax = 1.3 * 0.693, KmKo = 1.5, IpCamax = 0.6 * 0.05, KmpCa = 0.0005;
+  const double GCab = 3.3 * 7.684e-5, GNab = 0.001;
+  const double KSR = 1.0;
+  const double vmaxf = 1.53 * 137.0e-6, vmaxr = 1.53 * 137.0e-6;
+  const double KvScale = 1.13 * 1.03 * 1.55, Kv43Frac = 0.77;
+  const double GKv43 = Kv43Frac * KvScale * 0.1;
+  const double PKv14 = (1.0 - Kv43Frac) * KvScale * 4.792933e-7;
+  const double alphaa0Kv43 = 0.543708, betaa0Kv43 = 0.080185;
+  const double alphai0Kv43 = 0.0498424, betai0Kv43 = 0.000819482;
+  const double alphaa0Kv14 = 6.0 * 0.31551, betaa0Kv14 = 6.0 * 0.001966;
+  const double alphai0Kv14 = 6.0 * 0.0004938, betai0Kv14 = 6.0 * 0.0000176;
+  const double f1Kv43 = 1.8936, f2Kv43 = 14.224647456, f3Kv43 = 158.574378389, f4Kv43 = 142.936645351;
+  const double b1Kv43 = 6.77348, b2Kv43 = 15.6212705152, b3Kv43 = 28.7532603313, b4Kv43 = 524.576206679;
+  const double f1Kv14 = 0.20005, f2Kv14 = 0.320280, f3Kv14 = 13.50909223, f4Kv14 = 1151.7651385;
+  const double b1Kv14 = 2.2300, b2Kv14 = 12.000299, b3Kv14 = 5.3701338025, b4Kv14 = 5.2396395511;
+  const double T_Const_HERG = 5.320000001;
+  const double A0_HERG = 0.017147641733086, A1_HERG = 0.03969328381141, A2_HERG = 0.02057448605977;
+  const double A3_HERG = 0.00134366604423, A4_HERG = 0.10666316491288, A5_HERG = 0.00646393910049;
+  const double A6_HERG = 0.00008039374403;
+  const double C2H_to_C3H = T_Const_HERG * 0.02608362043337;
+  const double C3H_to_C2H = T_Const_HERG * 0.14832978132145;
+  const double RT_over_F = GWC_RT_over_F, Faraday = GWC_Faraday, Ko = GWC_Ko, Nao = GWC_Nao, Cao = GWC_Cao;
+  const double Acap = GWC_Acap, Vmyo = GWC_Vmyo, VNSR = GWC_VNSR, VJSR = GWC_VJSR, VSS = GWC_VSS;
+
+  double V, mNa = state[GW_mNa], hNa = state[GW_hNa], jNa = state[GW_jNa], Nai = state[GW_Nai];
+  double Ki = state[GW_Ki], Cai = state[GW_Cai], xKs = state[GW_xKs];
+  double LTRPNCa = state[GW_LTRPNCa], HTRPNCa = state[GW_HTRPNCa];
+  const double C0Kv43 = state[GW_C0Kv43], C1Kv43 = state[GW_C1Kv43], C2Kv43 = state[GW_C2Kv43];
+  const double C3Kv43 = state[GW_C3Kv43], OKv43 = state[GW_OKv43], CI0Kv43 = state[GW_CI0Kv43];
+  const double CI1Kv43 = state[GW_CI1Kv43], CI2Kv43 = state[GW_CI2Kv43], CI3Kv43 = state[GW_CI3Kv43];
+  const double OIKv43 = 1.0 - CI0Kv43 - CI1Kv43 - CI2Kv43 - CI3Kv43 - OKv43 - C0Kv43 - C1Kv43 - C2Kv43 - C3Kv43;
+  const double C0Kv14 = state[GW_C0Kv14], C1Kv14 = state[GW_C1Kv14], C2Kv14 = state[GW_C2Kv14];
+  const double C3Kv14 = state[GW_C3Kv14], OKv14 = state[GW_OKv14], CI0Kv14 = state[GW_CI0Kv14];
+  const double CI1Kv14 = state[GW_CI1Kv14], CI2Kv14 = state[GW_CI2Kv14], CI3Kv14 = state[GW_CI3Kv14];
+  const double OIKv14 = 1.0 - CI0Kv14 - CI1Kv14 - CI2Kv14 - CI3Kv14 - OKv14 - C0Kv14 - C1Kv14 - C2Kv14 - C3Kv14;
+  const double C1Herg = state[GW_C1Herg], C2Herg = state[GW_C2Herg], C3Herg = state[GW_C3Herg];
+  const double OHerg = state[GW_OHerg];
+  const double IHerg = 1.0 - OHerg - C1Herg - C2Herg - C3Herg;
+  double Istim, a1, a2, a3, a4, a5;
+  V = gw_fcn_voltage(time, state, P, &Istim);
+
   /* ---- reversal potentials, fcn.c:549-559 ---- */
-  const double ENa = RT_over_F * log(Nao / Nai);
-  const double EK = RT_over_F * log(Ko / Ki);
+  const double ENa = RT_over_F * tx->lg[0];
+  const double EK = RT_over_F * tx->lg[1];
   a1 = Ko + 0.01833 * Nao;
   a2 = Ki + 0.01833 * Nai;
-  const double EKs = RT_over_F * log(a1 / a2);
+  const double EKs = RT_over_F * tx->lg[2];
   if (Cai <= 0.0) Cai = 1.e-15;
-  const double ECa = 0.5 * RT_over_F * log(Cao / Cai);
+  const double ECa = 0.5 * RT_over_F * tx->lg[3];
 
   /* ---- INa, IKr, IKs, Ito1, IK1, INab, IKp, fcn.c:565-619 ---- */
   if (mNa <= 0.0) mNa = 1.e-15;
   const double INa = GNa * (mNa * mNa * mNa) * hNa * jNa * (V - ENa);
-  const double fKo = pow(Ko / 4.0, 0.5);
+  const double fKo = tx->pw[0];
   const double IKr = GKr * fKo * OHerg * (V - EK);
   const double IKs = GKs * (xKs * xKs) * (V - EKs);
   double IKv43 = GKv43 * OKv43 * (V - EK);
   double VF_over_RT = V / RT_over_F;
   const double VFsq_over_RT = (1000.0 * Faraday) * VF_over_RT;
-  const double exp_VFRT = exp(VF_over_RT);
+  const double exp_VFRT = tx->x[GW_X_VFRT];
   double IKv14_K, IKv14_Na;
   a1 = Ki * exp_VFRT - Ko;
   a2 = exp_VFRT - 1.0;
@@ -231,22 +346,22 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
   else IKv14_Na = 0.02 * PKv14 * OKv14 * VFsq_over_RT * (a1 / a2);
   const double IKv14 = IKv14_K + IKv14_Na;
   double Ito1 = IKv43 + IKv14;
-  const double K1_inf = 1.0 / (0.94 + exp(1.76 / RT_over_F * (V - EK)));
+  const double K1_inf = 1.0 / (0.94 + tx->k1);
   double IK1 = GK1 * Ko / (Ko + KmK1) * K1_inf * (V - EK);
   const double INab = GNab * (V - ENa);
-  const double KpV = 1.0 / (1.0 + exp((7.488 - V) / 5.98));
+  const double KpV = 1.0 / (1.0 + tx->x[GW_X_KPV]);
   const double IKp = GKp * KpV * (V - EK);
 
   /* ---- INaK, INaCa, ICab, IpCa, fcn.c:623-649 ---- */
   VF_over_RT = V / RT_over_F;
-  const double sigma = (exp(Nao / 67.3) - 1.0) / 7.0;
-  a1 = 1.0 + 0.1245 * exp(-0.1 * VF_over_RT);
+  const double sigma = (tx->x[GW_X_SIGMA] - 1.0) / 7.0;
+  a1 = 1.0 + 0.1245 * tx->x[GW_X_NAK];
   a2 = 0.0365 * sigma / exp_VFRT;
   const double fNaK = 1.0 / (a1 + a2);
   a1 = Ko / (Ko + KmKo);
-  a2 = 1.0 + pow(KmNai / Nai, 1.5);
+  a2 = 1.0 + tx->pw[1];
   const double INaK = INaKmax * fNaK * (a1 / a2);
-  const double exp_etaVFRT = exp(eta * VF_over_RT);
+  const double exp_etaVFRT = tx->x[GW_X_ETA];
   a1 = exp_etaVFRT * (Nai * Nai * Nai) * Cao;
   a2 = exp_etaVFRT / exp_VFRT * (Nao * Nao * Nao) * Cai;
   a3 = 1.0 + ksat * exp_etaVFRT / exp_VFRT;
@@ -262,9 +377,9 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
     alpha_m = 0.32 / (0.1 - 0.005 * (V + 47.13));
   } else {
     a1 = 0.32 * (V + 47.13);
-    alpha_m = a1 / (1.0 - exp(-0.1 * (V + 47.13)));
+    alpha_m = a1 / (1.0 - tx->x[GW_X_AM]);
   }
-  const double beta_m = 0.08 * exp(-V / 11.0);
+  const double beta_m = 0.08 * tx->x[GW_X_BM];
   if (V >= -90.0) {
     dmNa = alpha_m * (1.0 - mNa) - beta_m * mNa;
   } else {
@@ -272,31 +387,31 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
     mNa = alpha_m / (alpha_m + beta_m);
     state[GW_mNa] = mNa;
   }
-  const double alpha_h = 0.135 * exp((80 + V) / -6.8);
+  const double alpha_h = 0.135 * tx->x[GW_X_AH];
   double beta_h, alpha_j, beta_j;
-  if (V < -38.73809636838782) beta_h = 3.56 * exp(0.079 * V) + 310000 * exp(0.35 * V);
-  else beta_h = 1 / (0.13 * (1 + exp((V + 10.66) / -11.1)));
+  if (V < -38.73809636838782) beta_h = 3.56 * tx->x[GW_X_BH1] + 310000 * tx->x[GW_X_BH2];
+  else beta_h = 1 / (0.13 * (1 + tx->x[GW_X_BH3]));
   if (V < -37.78) {
-    a1 = -127140 * exp(0.2444 * V);
-    a2 = 3.474E-5 * exp(-0.04391 * V);
-    a3 = 1.0 + exp(0.311 * (V + 79.23));
+    a1 = -127140 * tx->x[GW_X_AJ1];
+    a2 = 3.474E-5 * tx->x[GW_X_AJ2];
+    a3 = 1.0 + tx->x[GW_X_AJ3];
     alpha_j = (a1 - a2) * (V + 37.78) / a3;
   } else {
     alpha_j = 0;
   }
-  if (V < -39.82600037702883) beta_j = 0.1212 * exp(-0.01052 * V) / (1.0 + exp(-0.1378 * (V + 40.14)));
-  else beta_j = 0.3 * exp(-2.535E-7 * V) / (1 + exp(-0.1 * (V + 32)));
+  if (V < -39.82600037702883) beta_j = 0.1212 * tx->x[GW_X_BJ1] / (1.0 + tx->x[GW_X_BJ2]);
+  else beta_j = 0.3 * tx->x[GW_X_BJ3] / (1 + tx->x[GW_X_BJ4]);
   const double dhNa = alpha_h * (1.0 - hNa) - beta_h * hNa;
   const double djNa = alpha_j * (1.0 - jNa) - beta_j * jNa;
 
   /* HERG Markov model (IKr) */
-  const double C1H_to_C2H = T_Const_HERG * A0_HERG * exp(B0_HERG * V);
-  const double C2H_to_C1H = T_Const_HERG * A1_HERG * exp(B1_HERG * V);
-  const double C3H_to_OH = T_Const_HERG * A2_HERG * exp(B2_HERG * V);
-  const double OH_to_C3H = T_Const_HERG * A3_HERG * exp(B3_HERG * V);
-  const double OH_to_IH = T_Const_HERG * A4_HERG * exp(B4_HERG * V);
-  const double IH_to_OH = T_Const_HERG * A5_HERG * exp(B5_HERG * V);
-  const double C3H_to_IH = T_Const_HERG * A6_HERG * exp(B6_HERG * V);
+  const double C1H_to_C2H = T_Const_HERG * A0_HERG * tx->x[GW_X_H0];
+  const double C2H_to_C1H = T_Const_HERG * A1_HERG * tx->x[GW_X_H1];
+  const double C3H_to_OH = T_Const_HERG * A2_HERG * tx->x[GW_X_H2];
+  const double OH_to_C3H = T_Const_HERG * A3_HERG * tx->x[GW_X_H3];
+  const double OH_to_IH = T_Const_HERG * A4_HERG * tx->x[GW_X_H4];
+  const double IH_to_OH = T_Const_HERG * A5_HERG * tx->x[GW_X_H5];
+  const double C3H_to_IH = T_Const_HERG * A6_HERG * tx->x[GW_X_H6];
   const double IH_to_C3H = (OH_to_C3H * IH_to_OH * C3H_to_IH) / (C3H_to_OH * OH_to_IH);
   const double dC1Herg = C2H_to_C1H * C2Herg - C1H_to_C2H * C1Herg;
   a1 = C1H_to_C2H * C1Herg + C3H_to_C2H * C3Herg;
@@ -310,28 +425,28 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
   const double dOHerg = a1 - a2;
 
   /* IKs */
-  const double xKs_inf = 1.0 / (1.0 + exp(-(V - 24.7) / 13.6));
+  const double xKs_inf = 1.0 / (1.0 + tx->x[GW_X_XKS]);
   if (fabs(V - 10) < 1.e-6) {
     a1 = (7.19e-5) / 0.148;
     a2 = (1.31e-4) / 0.0687;
   } else {
-    a1 = 7.19e-5 * (V - 10.0) / (1.0 - exp(-0.148 * (V - 10.0)));
-    a2 = 1.31e-4 * (V - 10.0) / (exp(0.0687 * (V - 10.0)) - 1.0);
+    a1 = 7.19e-5 * (V - 10.0) / (1.0 - tx->x[GW_X_KS1]);
+    a2 = 1.31e-4 * (V - 10.0) / (tx->x[GW_X_KS2] - 1.0);
   }
   const double tau_xKs = 1.0 / (a1 + a2);
   const double dxKs = (xKs_inf - xKs) / tau_xKs;
 
   /* ---- SR uptake and troponin, fcn.c:759-776 ---- */
-  const double fb = pow(Cai / Kfb, Nfb);
-  const double rb = pow(CaNSR / Krb, Nrb);
+  const double fb = tx->pw[2];
+  const double rb = tx->pw[3];
   double Jup = KSR * (vmaxf * fb - vmaxr * rb) / (1.0 + fb + rb);
   a1 = GWC_kltrpn_minus * LTRPNCa;
   const double dLTRPNCa = GWC_kltrpn_plus * Cai * (1.0 - LTRPNCa) - a1;
   a1 = GWC_khtrpn_minus * HTRPNCa;
   const double dHTRPNCa = GWC_khtrpn_plus * Cai * (1.0 - HTRPNCa) - a1;
   const double Jtrpn = GWC_LTRPNtot * dLTRPNCa + GWC_HTRPNtot * dHTRPNCa;
-  a1 = GWC_CMDNtot * GWC_KmCMDN / (pow(Cai + GWC_KmCMDN, 2.0));
-  a2 = GWC_EGTAtot * GWC_KmEGTA / (pow(Cai + GWC_KmEGTA, 2.0));
+  a1 = GWC_CMDNtot * GWC_KmCMDN / (tx->pw[4]);
+  a2 = GWC_EGTAtot * GWC_KmEGTA / (tx->pw[5]);
   const double beta_i = 1.0 / (1.0 + a1 + a2);
 
   /* ---- heart-failure scalings, fcn.c:780-786 ---- */
@@ -372,8 +487,8 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
 
   /* ---- Kv4.3, fcn.c:846-917 ---- */
   {
-    const double al = alphaa0Kv43 * exp(aaKv43 * V), be = betaa0Kv43 * exp(-baKv43 * V);
-    const double ali = alphai0Kv43 * exp(-aiKv43 * V), bei = betai0Kv43 * exp(biKv43 * V);
+    const double al = alphaa0Kv43 * tx->x[GW_X_43A], be = betaa0Kv43 * tx->x[GW_X_43B];
+    const double ali = alphai0Kv43 * tx->x[GW_X_43C], bei = betai0Kv43 * tx->x[GW_X_43D];
     const double C0C1 = 4.0 * al, C1C2 = 3.0 * al, C2C3 = 2.0 * al, C3O = al;
     const double CI0CI1 = 4.0 * b1Kv43 * al, CI1CI2 = 3.0 * b2Kv43 * al / b1Kv43;
     const double CI2CI3 = 2.0 * b3Kv43 * al / b2Kv43, CI3OI = b4Kv43 * al / b3Kv43;
@@ -401,7 +516,7 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
   }
   /* ---- Kv1.4, fcn.c:927-998 ---- */
   {
-    const double al = alphaa0Kv14 * exp(aaKv14 * V), be = betaa0Kv14 * exp(-baKv14 * V);
+    const double al = alphaa0Kv14 * tx->x[GW_X_14A], be = betaa0Kv14 * tx->x[GW_X_14B];
     const double ali = alphai0Kv14, bei = betai0Kv14;
     const double C0C1 = 4.0 * al, C1C2 = 3.0 * al, C2C3 = 2.0 * al, C3O = al;
     const double CI0CI1 = 4.0 * b1Kv14 * al, CI1CI2 = 3.0 * b2Kv14 * al / b1Kv14;
@@ -446,6 +561,30 @@ GW_HD void gw_fcn(const double time, double* state, double* F, double* current, 
     current[GW_I_IKv14_Na] = IKv14_Na; current[GW_I_Ito2] = Ito2; current[GW_I_Istim] = Istim;
     current[GW_I_Itot] = Itot;
   }
+}
+
+/* The transcendental terms for the state at `time`, one after another. */
+GW_HD void gw_tx_fill(const double time, const double* state, const gw_protocol* P, gw_tx* tx) {
+  double Istim;
+  const double V = gw_fcn_voltage(time, state, P, &Istim);
+  int k;
+  for (k = 0; k < GW_NX; k++) tx->x[k] = exp(gw_x_arg(k, V));
+  for (k = 0; k < 4; k++) tx->lg[k] = log(gw_lg_arg(k, state));
+  for (k = 0; k < 6; k++) {
+    double y;
+    const double b = gw_pw_arg(k, state, &y);
+    tx->pw[k] = pow(b, y);
+  }
+  tx->k1 = exp(gw_k1_arg(V, tx->lg));
+}
+
+/* Global right-hand side (fcn.c:29-1072): gw_fcn_tx with the terms
+ * evaluated in turn. */
+GW_HD void gw_fcn(const double time, double* state, double* F, double* current, const int keepc,
+                  const double Jxfer, const double Jtr, const double ICa, const double Ito2, const gw_protocol* P) {
+  gw_tx tx;
+  gw_tx_fill(time, state, P, &tx);
+  gw_fcn_tx(time, state, F, current, keepc, Jxfer, Jtr, ICa, Ito2, P, &tx);
 }
 
 /* Rest state of initialize_state.c:167-203 (37 globals). */

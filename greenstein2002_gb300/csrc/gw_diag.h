@@ -15,6 +15,14 @@ extern "C" {
  * GPU thread and on the host: what a device-resident integrator pays per
  * stage on GB300's FP64 rate. */
 int gw_probe_fcn(double *device_us, double *host_us);
+/* The same cost with the whole warp: fcn's exponentials, logs and powers
+ * one per lane, then the arithmetic that combines them. */
+int gw_probe_fcn_warp(double *us);
+/* fcn of n states (states[n][37]) at `time` (clamp != 0: under a -100 / 0
+ * mV voltage clamp) on one GPU thread and on a warp: derivatives
+ * Fs/Fw[n][37] and currents Cs/Cw[n][24] of both. */
+int gw_probe_fcn_compare(const double *states, int n, double time, int clamp, double *Fs, double *Fw, double *Cs,
+                         double *Cw);
 /* exp() of n arguments as the device evaluates it and with the host libm:
  * exp is the FRU path's only transcendental, and the two may round
  * differently in the last place. */

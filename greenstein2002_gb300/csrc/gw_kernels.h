@@ -132,6 +132,10 @@ cudaError_t probe_exp(const double* x, double* device_y, double* host_y, int n);
 cudaError_t probe_fp64_issue(double* cycles);
 // gw_div_rn against the hardware division on n device-drawn operand pairs.
 cudaError_t probe_div(unsigned long long seed, long long n, unsigned long long* mismatches);
+// fcn on one thread against fcn on a warp, for n states; and the warp's cost
+cudaError_t probe_fcn_compare(const double* states, int n, double time, int clamp, double* Fs, double* Fw,
+                              double* Cs, double* Cw);
+cudaError_t probe_fcn_warp(double* us);
 cudaError_t launch_seed(const DevState& s, int scheme, uint32_t base, cudaStream_t st);
 
 }  // namespace gw

@@ -20,8 +20,10 @@
 //                  operations that do not advance; the warp that finishes
 //                  the last chunk adds the partials in the fixed order of
 //                  cell_finish, forms the currents, runs the cell's
-//                  integrator step (dp_after, the arithmetic of gw_dp.c) and
-//                  posts the cell's next operation.
+//                  integrator step on the whole warp (dp_after_warp: the
+//                  arithmetic of gw_dp.c, the 37-state vectors split over
+//                  the lanes and fcn's exponentials one per lane) and posts
+//                  the cell's next operation.
 // A warp whose groups find nothing to take works on whatever else is open,
 // so one cell's slowest FRU no longer holds the GPU: other cells' FRUs fill
 // the idle lanes.  Every cell's arithmetic, reduction order and integrator
@@ -208,13 +210,21 @@ __device__ __forceinline__ void finish_op(const Args& a, int ci, int lane) {
 #pragma unroll
     for (int k = 0; k < NV; k++) tot[k] += __ldcg(&s.partials[b * NV + k]);
   cleft::warp_sum<NV>(tot);
+#pragma unroll
+  for (int k = 0; k < NV; k++) tot[k] = __shfl_sync(kFull, tot[k], 0);
+  PCell& pc = a.pc[ci];
+  double cur[4];
+  currents_from_sums(s.nfru, c.sp.nfru_scale, c.sp.depf, tot, cur);
+  cur[2] = cur[2] * c.sp.pca_scale;  // ICa is proportional to the LCC permeability
+  const bool ovf = vload(&pc.overflow) != 0u;
+  __syncwarp();
+  if (ovf) {
+    if (lane == 0) c.err = 1;  // substep limit: corrupted FRU state
+    __syncwarp();
+  } else {
+    dp_after_warp(c, cur, NV == 16 ? tot + 5 : nullptr, lane);
+  }
   if (lane == 0) {
-    PCell& pc = a.pc[ci];
-    double cur[4];
-    currents_from_sums(s.nfru, c.sp.nfru_scale, c.sp.depf, tot, cur);
-    cur[2] = cur[2] * c.sp.pca_scale;  // ICa is proportional to the LCC permeability
-    if (vload(&pc.overflow)) c.err = 1;  // substep limit: corrupted FRU state
-    else dp_after(c, cur, NV == 16 ? tot + 5 : nullptr);
     atomicAdd(a.ops, 1ull);
     if (c.done || c.err) {
       pc.finished = 1;

@@ -6,6 +6,7 @@
 #include <chrono>
 
 #include "gw_cell_model.h"
+#include "gw_dp_device.cuh"
 #include "gw_intdiv.h"
 #include "gw_kernels.h"
 
@@ -289,6 +290,109 @@ cudaError_t probe_div(unsigned long long seed, long long n, unsigned long long* 
   }
   if (e == cudaSuccess) e = cudaMemcpy(mismatches, d, sizeof *d, cudaMemcpyDeviceToHost);
   cudaFree(d);
+  return e;
+}
+
+// fcn of n states at `time`: one thread (gw_fcn) against a whole warp
+// (the transcendental terms one per lane, tx_fill_warp, then gw_fcn_tx on
+// every lane); derivatives and currents of both, for a bit-for-bit check.
+__global__ void fcn_compare_kernel(const double* states, int n, const gw_protocol* P, double time, double* Fs,
+                                   double* Fw, double* Cs, double* Cw) {
+  __shared__ gw_tx tx;
+  const int i = blockIdx.x, lane = threadIdx.x;
+  if (i >= n) return;
+  double y[GW_NSTATE], F[GW_NSTATE], cur[GW_NCUR];
+  for (int k = 0; k < GW_NSTATE; k++) y[k] = states[(size_t)i * GW_NSTATE + k];
+  if (lane == 0) {
+    double ys[GW_NSTATE];
+    for (int k = 0; k < GW_NSTATE; k++) ys[k] = y[k];
+    gw_fcn(time, ys, F, cur, 1, 2e-6, 1e-6, -2e-3, 1e-4, P);
+    for (int k = 0; k < GW_NSTATE; k++) Fs[(size_t)i * GW_NSTATE + k] = F[k];
+    for (int k = 0; k < GW_NCUR; k++) Cs[(size_t)i * GW_NCUR + k] = cur[k];
+  }
+  __syncwarp();
+  tx_fill_warp(time, y, P, &tx, lane);
+  gw_fcn_tx(time, y, F, cur, 1, 2e-6, 1e-6, -2e-3, 1e-4, P, &tx);
+  if (lane == 0) {
+    for (int k = 0; k < GW_NSTATE; k++) Fw[(size_t)i * GW_NSTATE + k] = F[k];
+    for (int k = 0; k < GW_NCUR; k++) Cw[(size_t)i * GW_NCUR + k] = cur[k];
+  }
+}
+
+cudaError_t probe_fcn_compare(const double* states, int n, double time, int clamp, double* Fs, double* Fw,
+                              double* Cs, double* Cw) {
+  gw_protocol hp;
+  gw_protocol_defaults(&hp);
+  if (clamp) {
+    hp.vclamp_flag = 1;
+    hp.vclamp_hold = -100.0;
+    hp.vclamp_set = 0.0;
+    hp.vclamp_shift = 0.0;
+    hp.vclamp_duration = 200.0;
+  }
+  gw_protocol* dp = nullptr;
+  double* d = nullptr;
+  const size_t ns = (size_t)n * GW_NSTATE, nc = (size_t)n * GW_NCUR;
+  cudaError_t e = cudaMalloc(&dp, sizeof hp);
+  if (e == cudaSuccess) e = cudaMalloc(&d, sizeof(double) * (3 * ns + 2 * nc));
+  if (e == cudaSuccess) e = cudaMemcpy(dp, &hp, sizeof hp, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d, states, sizeof(double) * ns, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    fcn_compare_kernel<<<n, 32>>>(d, n, dp, time, d + ns, d + 2 * ns, d + 3 * ns, d + 3 * ns + nc);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(Fs, d + ns, sizeof(double) * ns, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Fw, d + 2 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Cs, d + 3 * ns, sizeof(double) * nc, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(Cw, d + 3 * ns + nc, sizeof(double) * nc, cudaMemcpyDeviceToHost);
+  cudaFree(dp);
+  cudaFree(d);
+  return e;
+}
+
+// Microseconds per fcn evaluation on one warp (the transcendental terms one
+// per lane), `calls` dependent evaluations as fcn_chain.
+__global__ void fcn_chain_warp(const gw_protocol* P, int calls, double* out) {
+  __shared__ gw_tx tx;
+  const int lane = threadIdx.x;
+  double y[GW_NSTATE], F[GW_NSTATE], cur[GW_NCUR];
+  gw_rest_state(y);
+  for (int i = 0; i < calls; i++) {
+    tx_fill_warp(10.5, y, P, &tx, lane);
+    gw_fcn_tx(10.5, y, F, cur, 1, 1e-6, 1e-6, -1e-3, 0.0, P, &tx);
+    y[GW_V] = y[GW_V] + fcn_feedback(F, cur);
+    __syncwarp();
+  }
+  if (lane == 0) out[0] = y[GW_V];
+}
+
+cudaError_t probe_fcn_warp(double* us) {
+  const int calls = 200;
+  gw_protocol hp;
+  gw_protocol_defaults(&hp);
+  gw_protocol* dp = nullptr;
+  double* out = nullptr;
+  cudaEvent_t e0, e1;
+  cudaError_t e = cudaMalloc(&dp, sizeof hp);
+  if (e == cudaSuccess) e = cudaMalloc(&out, sizeof(double));
+  if (e == cudaSuccess) e = cudaMemcpy(dp, &hp, sizeof hp, cudaMemcpyHostToDevice);
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3 && e == cudaSuccess; rep++) {
+    cudaEventRecord(e0);
+    fcn_chain_warp<<<1, 32>>>(dp, calls, out);
+    cudaEventRecord(e1);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && rep > 0) best = ms < best ? ms : best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(dp);
+  cudaFree(out);
+  *us = 1e3 * best / calls;
   return e;
 }
 

@@ -84,3 +84,24 @@ def test_persistent_wait_limit_returns_an_error_status(gw):
     st = states[0].copy()
     t, tr, _, _ = cells[0].run(st, 0.0, 2, set_=sets[0], want=("states",))
     assert t == 2.0 and np.all(np.isfinite(tr))
+
+
+def test_warp_fcn_same_bits_as_one_thread(gw):
+    """The warp form of the global right-hand side (its exponentials, logs
+    and powers one per lane) returns the one-thread form's derivatives and
+    currents bit for bit, over states spread around the action potential and
+    under a voltage clamp."""
+    rng = np.random.default_rng(11)
+    cell = gw.Cell(50)
+    rest = cell.init_rest(gw.settings(), scheme=gw.SEED_BASE, base=1)
+    cell.close()
+    n = 512
+    st = np.tile(rest, (n, 1))
+    st[:, 0] = rng.uniform(-100.0, 60.0, n)                # V across the action potential
+    st[:, 1:] *= rng.uniform(0.7, 1.3, (n, 36))             # gates and concentrations around rest
+    st[:5, 0] = [-47.13, 10.0, 0.0, -90.5, -38.7]          # the branch points of fcn
+    for time, clamp in ((5.0, False), (10.5, False), (120.0, True)):
+        Fs, Fw, Cs, Cw = gw.fcn_thread_vs_warp(st, time, clamp=clamp)
+        np.testing.assert_array_equal(Fs, Fw)
+        np.testing.assert_array_equal(Cs, Cw)
+    assert np.all(np.isfinite(Fs))
