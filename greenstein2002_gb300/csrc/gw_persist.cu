@@ -58,6 +58,8 @@ namespace gw {
 namespace persist {
 
 constexpr int kChunkGroups = 32;  // 8-FRU groups per reduction chunk (256 FRUs)
+constexpr int kTakeFrus = 4;      // FRUs a 4-lane group takes at once (one counter update, one fence)
+constexpr int kMaxCells = 1024;   // cells of one run (16 mask words)
 constexpr unsigned kFull = 0xffffffffu;
 enum : int { kStatusOk = 0, kStatusWatchdog = 3 };
 constexpr unsigned long long kDefaultWaitNs = 2000000000ull;
@@ -82,8 +84,9 @@ struct Args {
   PCell* pc;
   int ncells;
   unsigned* running;             // cells with output steps left
-  int* fru_open;                 // cells whose FRU phase has FRUs left to take (a hint)
-  int* red_open;                 // cells whose reduction has chunks left to take (a hint)
+  unsigned long long* fru_mask;  // bit per cell: its FRU phase has FRUs left to take
+  unsigned long long* red_mask;  // bit per cell: its reduction has chunks left to take
+  int nwords;                    // 64-bit words of each mask
   unsigned long long* progress;  // FRUs and chunks finished
   unsigned long long* ops;       // operations completed
   int* status;                   // kStatus*
@@ -98,12 +101,45 @@ __device__ __forceinline__ unsigned long long vload(const unsigned long long* p)
 }
 
 // ---- posting operations (one thread) -----------------------------------------------
+// A cell's bit in a mask is set after its counter is reset (open), and the
+// warp that finds the counter exhausted clears the bit and then looks at the
+// counter again, setting the bit back if a new phase opened meanwhile; so a
+// phase with work left always has its bit set.
+__device__ __forceinline__ void mask_set(unsigned long long* m, int ci) {
+  atomicOr(&m[ci >> 6], 1ull << (ci & 63));
+}
+__device__ __forceinline__ void mask_clear_fru(const Args& a, int ci) {
+  atomicAnd(&a.fru_mask[ci >> 6], ~(1ull << (ci & 63)));
+  __threadfence();
+  if (vload(&a.pc[ci].take) < (unsigned long long)a.cells[ci].nfru) mask_set(a.fru_mask, ci);
+}
+__device__ __forceinline__ void mask_clear_red(const Args& a, int ci) {
+  atomicAnd(&a.red_mask[ci >> 6], ~(1ull << (ci & 63)));
+  __threadfence();
+  if (vload(&a.pc[ci].red_take) < (unsigned)a.pc[ci].nchunks) mask_set(a.red_mask, ci);
+}
+// a set bit of the mask at or after `from` (cyclically); -1: none
+__device__ __forceinline__ int mask_pick(const unsigned long long* m, int nwords, int ncells, int from) {
+  const int w0 = from >> 6;
+  for (int k = 0; k <= nwords; k++) {
+    const int w = (w0 + k) % nwords;
+    unsigned long long bits = vload(&m[w]);
+    if (k == 0) bits &= ~0ull << (from & 63);
+    else if (k == nwords) bits &= ~(~0ull << (from & 63));
+    if (bits) {
+      const int ci = (w << 6) + __ffsll((long long)bits) - 1;
+      return ci < ncells ? ci : -1;
+    }
+  }
+  return -1;
+}
+
 static __device__ void open_reduction(const Args& a, int ci) {
   PCell& pc = a.pc[ci];
   pc.red_done = 0u;
   atomicExch(&pc.red_take, 0u);
   __threadfence();
-  atomicAdd(a.red_open, 1);
+  mask_set(a.red_mask, ci);
 }
 
 // Post the operation dp_after has just set up in the cell's DpCell.
@@ -115,7 +151,7 @@ static __device__ void post(const Args& a, int ci) {
   if (a.dp[ci].sp.flags & kFlagAdvance) {
     atomicExch(&pc.take, 0ull);
     __threadfence();
-    atomicAdd(a.fru_open, 1);
+    mask_set(a.fru_mask, ci);
   } else {
     open_reduction(a, ci);
   }
@@ -244,7 +280,7 @@ static __device__ bool reduce_chunk(const Args& a, int ci, const cleft::Group& g
   unsigned k = 0u;
   if (lane == 0) {
     k = atomicAdd(&pc.red_take, 1u);
-    if (k == (unsigned)pc.nchunks - 1u) atomicSub(a.red_open, 1);
+    if (k >= (unsigned)pc.nchunks - 1u) mask_clear_red(a, ci);
   }
   k = __shfl_sync(kFull, k, 0);
   if (k >= (unsigned)pc.nchunks) return false;
@@ -273,20 +309,11 @@ static __device__ bool reduce_chunk(const Args& a, int ci, const cleft::Group& g
   return true;
 }
 
-// A cell with reduction chunks left (warp-uniform; -1: none).  Lanes look at
-// cells lane, lane + 32, ... starting from `from`.
+// A cell with reduction chunks left (warp-uniform; -1: none).
 static __device__ int find_reduction(const Args& a, int from, int lane) {
-  for (int k0 = 0; k0 < a.ncells; k0 += 32) {
-    const int k = k0 + lane;
-    int ci = -1;
-    if (k < a.ncells) {
-      const int cj = (from + k) % a.ncells;
-      if (vload(&a.pc[cj].red_take) < (unsigned)a.pc[cj].nchunks) ci = cj;
-    }
-    const unsigned m = __ballot_sync(kFull, ci >= 0);
-    if (m) return __shfl_sync(kFull, ci, __ffs(m) - 1);
-  }
-  return -1;
+  int ci = -1;
+  if (lane == 0) ci = mask_pick(a.red_mask, a.nwords, a.ncells, from);
+  return __shfl_sync(kFull, ci, 0);
 }
 
 // MT19937 regeneration of the rows whose draws run past word 624 in this
@@ -347,7 +374,7 @@ __device__ __forceinline__ void persist_body(const Args& a) {
   F.mti = 0;
   LS.tf = 0.0;
   LS.interval = 0.0;
-  int ci = -1, f = -1, nfru = 0;
+  int ci = -1, f = -1, f_end = -1, nfru = 0, taken = 0;
   uint32_t epoch = 0u;
   bool ovf = false;
   const DevState* S = nullptr;
@@ -355,20 +382,53 @@ __device__ __forceinline__ void persist_body(const Args& a) {
   unsigned long long seen = 0ull, idle_since = 0ull;
   bool idle_clock = false;
 
-  // the next FRU of any open FRU phase (group-uniform; false: none)
+  // load FRU ff of the group's operation into the group's lanes
+  auto load = [&](int ff) {
+    const StageParams& p = a.dp[ci].sp;
+    f = ff;
+    sc.f = ff;
+    sc.my_hold_epoch = S->hold_epoch + ff;
+    const size_t nf = (size_t)S->stride;
+    bool restore = false;
+    if (p.flags & kFlagResume) {
+      F.jsr.set(S->frus_s[ff]);
+      F.ss.set(S->frus_s[(g.c + 1) * nf + ff]);
+      F.w = S->chan_s[g.c * nf + ff];
+      F.mti = S->mti_s[ff];
+      restore = (*sc.my_hold_epoch == epoch);
+    } else {
+      F.jsr.set(__ldcg(&S->frus[ff]));
+      F.ss.set(__ldcg(&S->frus[(g.c + 1) * nf + ff]));
+      F.w = __ldcg(&S->chan[g.c * nf + ff]);
+      F.mti = __ldcg(&S->mti[ff]);
+    }
+    if (p.flags & kFlagSave) {
+      if (g.c == 0) {
+        S->frus_s[ff] = F.jsr.get();
+        S->mti_s[ff] = F.mti;
+      }
+      S->frus_s[(g.c + 1) * nf + ff] = F.ss.get();
+      S->chan_s[g.c * nf + ff] = F.w;
+    }
+    copy_row16(sc.m, restore ? S->mt_hold + (size_t)ff * kMtStride : S->mt + (size_t)ff * kMtStride, g);
+    sc.dirty = restore;
+    F.nsub = 0u;
+    fru_begin(F, LS);
+  };
+  // the next kTakeFrus FRUs of any open FRU phase (group-uniform; false: none)
   auto take = [&]() -> bool {
     int got_c = -1, got_f = -1;
-    if (g.c == 0 && vload(a.fru_open) > 0) {
-      for (int k = 0; k < a.ncells; k++) {
-        const int cj = (cursor + k) % a.ncells;
+    if (g.c == 0) {
+      for (int tries = 0; tries < 4; tries++) {
+        const int cj = mask_pick(a.fru_mask, a.nwords, a.ncells, cursor);
+        if (cj < 0) break;
         const unsigned n = (unsigned)a.cells[cj].nfru;
-        if (vload(&a.pc[cj].take) >= (unsigned long long)n) continue;
-        const unsigned idx = (unsigned)atomicAdd(&a.pc[cj].take, 1ull);
+        const unsigned idx = (unsigned)atomicAdd(&a.pc[cj].take, (unsigned long long)kTakeFrus);
+        if (idx + kTakeFrus >= n) mask_clear_fru(a, cj);  // the phase has no FRUs left to take
+        cursor = cj;
         if (idx >= n) continue;
-        if (idx == n - 1u) atomicSub(a.fru_open, 1);
         got_c = cj;
         got_f = (int)idx;
-        cursor = cj;
         break;
       }
     }
@@ -377,48 +437,22 @@ __device__ __forceinline__ void persist_body(const Args& a) {
     if (got_c < 0) return false;
     __threadfence();  // the operation's parameters after the take
     ci = got_c;
-    f = got_f;
     S = &a.cells[ci];
     nfru = S->nfru;
+    f_end = min(nfru, got_f + kTakeFrus);
+    taken = f_end - got_f;
     const StageParams& p = a.dp[ci].sp;
     lane_stage(p, g, LS);
     epoch = p.epoch;
     sc.p = &p;
-    sc.f = f;
     sc.hold_base = S->mt_hold;
     sc.hold_epoch_base = S->hold_epoch;
-    sc.my_hold_epoch = S->hold_epoch + f;
-    const size_t nf = (size_t)S->stride;
-    bool restore = false;
-    if (p.flags & kFlagResume) {
-      F.jsr.set(S->frus_s[f]);
-      F.ss.set(S->frus_s[(g.c + 1) * nf + f]);
-      F.w = S->chan_s[g.c * nf + f];
-      F.mti = S->mti_s[f];
-      restore = (*sc.my_hold_epoch == epoch);
-    } else {
-      F.jsr.set(__ldcg(&S->frus[f]));
-      F.ss.set(__ldcg(&S->frus[(g.c + 1) * nf + f]));
-      F.w = __ldcg(&S->chan[g.c * nf + f]);
-      F.mti = __ldcg(&S->mti[f]);
-    }
-    if (p.flags & kFlagSave) {
-      if (g.c == 0) {
-        S->frus_s[f] = F.jsr.get();
-        S->mti_s[f] = F.mti;
-      }
-      S->frus_s[(g.c + 1) * nf + f] = F.ss.get();
-      S->chan_s[g.c * nf + f] = F.w;
-    }
-    copy_row16(sc.m, restore ? S->mt_hold + (size_t)f * kMtStride : S->mt + (size_t)f * kMtStride, g);
-    sc.dirty = restore;
-    F.nsub = 0u;
     ovf = false;
-    fru_begin(F, LS);
+    load(got_f);
     return true;
   };
-  // store the group's FRU; the group that stores a phase's last FRU opens
-  // the reduction
+  // store the group's FRU and load the next one it holds; after its last,
+  // count them done -- the group that completes a phase opens the reduction
   auto finish = [&]() {
     const size_t nf = (size_t)S->stride;
     if (sc.dirty) copy_row16(S->mt + (size_t)f * kMtStride, sc.m, g);
@@ -429,18 +463,23 @@ __device__ __forceinline__ void persist_body(const Args& a) {
     }
     S->frus[(g.c + 1) * nf + f] = F.ss.get();
     S->chan[g.c * nf + f] = F.w;
+    if (f + 1 < f_end) {
+      __syncwarp(g.mask);
+      load(f + 1);
+      return;
+    }
     __threadfence();
     __syncwarp(g.mask);
     unsigned last = 0u;
     if (g.c == 0) {
       PCell& pc = a.pc[ci];
       if (ovf) atomicOr(&pc.overflow, 1u);
-      last = (atomicAdd(&pc.done, 1u) == (unsigned)nfru - 1u) ? 1u : 0u;
+      last = (atomicAdd(&pc.done, (unsigned)taken) + (unsigned)taken == (unsigned)nfru) ? 1u : 0u;
       if (last) {
         __threadfence();
         open_reduction(a, ci);
       }
-      atomicAdd(a.progress, 1ull);
+      atomicAdd(a.progress, (unsigned long long)taken);
     }
     __syncwarp(g.mask);
     ci = -1;
@@ -448,19 +487,18 @@ __device__ __forceinline__ void persist_body(const Args& a) {
   };
 
   while (true) {
-    int stop = 0;
-    if (lane == 0) stop = vload(a.status) != kStatusOk ? 2 : (vload(a.running) == 0u ? 1 : 0);
-    stop = __shfl_sync(kFull, stop, 0);
-    if (stop) break;  // an error, or every cell is done (no operation is open then)
-    bool worked = false;
-    // reduction chunks first: they are on a cell's critical path
-    int red = -1;
-    if (lane == 0) red = vload(a.red_open) > 0 ? 1 : 0;
-    if (__shfl_sync(kFull, red, 0)) {
-      const int rc = find_reduction(a, cursor, lane);
-      if (rc >= 0) worked = reduce_chunk(a, rc, g, lane);
+    // flags for the end of this iteration, loaded now so that their latency
+    // hides behind the substep
+    int st = kStatusOk;
+    unsigned run = 1u;
+    int red = 0;
+    if (lane == 0) {
+      st = vload(a.status);
+      run = vload(a.running);
+      for (int w = 0; w < a.nwords; w++) red |= vload(&a.red_mask[w]) != 0ull;
     }
-    // groups without an FRU take one
+    bool worked = false;
+    // groups without an FRU take some
     if (ci < 0) take();
     const bool has = ci >= 0;
     bool go = has && F.clk.running(LS);
@@ -484,6 +522,15 @@ __device__ __forceinline__ void persist_body(const Args& a) {
       worked = true;
     }
     __syncwarp();
+    st = __shfl_sync(kFull, st, 0);
+    run = __shfl_sync(kFull, run, 0);
+    if (st != kStatusOk) break;  // an error somewhere: every warp returns
+    if (run == 0u && !__any_sync(kFull, ci >= 0)) break;  // every cell is done
+    // reduction chunks: they are on a cell's critical path
+    if (__shfl_sync(kFull, red, 0)) {
+      const int rc = find_reduction(a, cursor, lane);
+      if (rc >= 0) worked = reduce_chunk(a, rc, g, lane) || worked;
+    }
     if (__any_sync(kFull, worked)) {
       idle_clock = false;
       continue;
@@ -504,7 +551,7 @@ __device__ __forceinline__ void persist_body(const Args& a) {
       }
     }
     if (__shfl_sync(kFull, give_up, 0)) break;
-    __nanosleep(2000);
+    __nanosleep(1000);
   }
 }
 
@@ -526,8 +573,8 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
                    int n_steps, double* state_trace, double* other_trace, double* cur_trace,
                    unsigned long long wait_ns, bool hold, int* status_out, unsigned long long* ops_out) {
   const char* who = "gw_run_persistent";
-  if (n <= 0 || !cells || !sets || !t || !states || !oldsteps || n_steps <= 0)
-    return gw_internal_error(GW_EINVAL, "gw_run_persistent: bad argument");
+  if (n <= 0 || n > gw::persist::kMaxCells || !cells || !sets || !t || !states || !oldsteps || n_steps <= 0)
+    return gw_internal_error(GW_EINVAL, "gw_run_persistent: bad argument (1 to 1024 cells)");
   const int prec = cells[0]->precision;
   for (int i = 0; i < n; i++)
     if (!cells[i] || cells[i]->precision != prec || cells[i]->fru_lanes != 4 || cells[i]->batch ||
@@ -582,8 +629,10 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   gw::DevState* dcells = nullptr;
   DpCell* ddp = nullptr;
   PCell* dpc = nullptr;
-  // counters: [0] running, [1] fru_open, [2] red_open, [3] status, [4] release; then progress, ops
+  // counters: [0] running, [3] status, [4] release; then progress, ops; the two cell masks
   int* dcnt = nullptr;
+  unsigned long long* dmask = nullptr;
+  const int nwords = (n + 63) / 64;
   unsigned long long* d64 = nullptr;
   double *dst = nullptr, *dot = nullptr, *dcu = nullptr;
   DpCell* hout = nullptr;  // pinned copy-back of the integrators
@@ -608,6 +657,7 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   if (e == cudaSuccess) e = cudaMalloc(&ddp, sizeof(DpCell) * n);
   if (e == cudaSuccess) e = cudaMalloc(&dpc, sizeof(PCell) * n);
   if (e == cudaSuccess) e = cudaMalloc(&dcnt, sizeof(int) * 8);
+  if (e == cudaSuccess) e = cudaMalloc(&dmask, sizeof(unsigned long long) * 2 * nwords);
   if (e == cudaSuccess) e = cudaMalloc(&d64, sizeof(unsigned long long) * 2);
   if (e == cudaSuccess) e = cudaMallocHost(&hout, sizeof(DpCell) * n);
   if (e == cudaSuccess && state_trace) e = cudaMalloc(&dst, sizeof(double) * ns * GW_NSTATE);
@@ -624,6 +674,12 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   if (e == cudaSuccess) e = cudaMemcpy(ddp, hdp.data(), sizeof(DpCell) * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dpc, hpc.data(), sizeof(PCell) * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dcnt, cnt, sizeof cnt, cudaMemcpyHostToDevice);
+  {
+    // no FRU phase open; every cell's first operation (a flux) is in its reduction
+    std::vector<unsigned long long> m(2 * nwords, 0ull);
+    for (int i = 0; i < n; i++) m[nwords + (i >> 6)] |= 1ull << (i & 63);
+    if (e == cudaSuccess) e = cudaMemcpy(dmask, m.data(), sizeof(unsigned long long) * m.size(), cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) e = cudaMemset(d64, 0, sizeof(unsigned long long) * 2);
   gw::persist::Args args;
   args.cells = dcells;
@@ -631,8 +687,9 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   args.pc = dpc;
   args.ncells = n;
   args.running = (unsigned*)dcnt;
-  args.fru_open = dcnt + 1;
-  args.red_open = dcnt + 2;
+  args.fru_mask = dmask;
+  args.red_mask = dmask + nwords;
+  args.nwords = nwords;
   args.status = dcnt + 3;
   args.release = hold ? dcnt + 4 : nullptr;
   args.progress = d64;
@@ -689,6 +746,7 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   cudaFree(ddp);
   cudaFree(dpc);
   cudaFree(dcnt);
+  cudaFree(dmask);
   cudaFree(d64);
   cudaFree(dst);
   cudaFree(dot);
