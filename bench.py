@@ -148,8 +148,9 @@ def parse():
                     help="Poisson arrival rates (req/s) of the serving sweep")
     ap.add_argument("--serve-requests", type=int, default=16,
                     help="requests per rate (at most rate x 24 s of arrivals, at least 16)")
-    ap.add_argument("--serve-ms", type=float, default=0.0,
-                    help="cap on each request's simulated ms (0: the full protocol, 1-10 beats or the 200-ms step)")
+    ap.add_argument("--serve-ms", type=float, default=1000.0,
+                    help="cap on each request's simulated ms: the default 1000 keeps the clamp run whole and the "
+                         "first second of a paced one; 0 runs every request's whole protocol (1-10 beats, minutes)")
     ap.add_argument("--serve-slots", type=int, default=32)
     ap.add_argument("--serve-budget-gb", type=float, default=64.0)
     ap.add_argument("--fru-lanes", type=int, default=4, choices=[1, 4],

@@ -34,7 +34,6 @@
 
 #include "gw_fru_core.cuh"
 #include "gw_fru_model.cuh"
-#include "gw_intdiv.h"
 #include "gw_kernels.h"
 
 namespace gw {
@@ -64,13 +63,15 @@ __device__ __forceinline__ double divc(double x, double d, double r) {
   return fma(fma(-q, d, x), r, q);
 }
 __device__ __forceinline__ float divc(float x, float d, float r) { return x * r; }
-// Divisions by variable divisors.  FP64: the correctly rounded quotient
-// computed on the integer pipe (gw_intdiv.h), the same bits as a / b
-// without the ~6 FP64-pipe slots of the hardware sequence.  FP32: rdiv is
-// the fast approximate quotient, qdiv the correctly rounded one.
-__device__ __forceinline__ double rdiv(double a, double b) { return gw_div_rn(a, b); }
+// Divisions by variable divisors.  FP64: the hardware's correctly rounded
+// quotient.  (The integer-pipe division of gw_intdiv.h gives the same bits
+// with ~6 fewer FP64-pipe slots, but its longer dependent chain made the
+// latency-bound stage kernels 25-30% slower on GB300, so it is not used
+// here.)  FP32: rdiv is the fast approximate quotient, qdiv the correctly
+// rounded one.
+__device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
-__device__ __forceinline__ double qdiv(double a, double b) { return gw_div_rn(a, b); }
+__device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float qdiv(float a, float b) { return a / b; }
 __device__ __forceinline__ double rexp(double x) { return exp(x); }
 __device__ __forceinline__ float rexp(float x) { return expf(x); }

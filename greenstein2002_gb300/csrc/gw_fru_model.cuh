@@ -10,8 +10,6 @@
 #pragma once
 #include <stdint.h>
 
-#include "gw_intdiv.h"
-
 namespace gw {
 
 constexpr int kClefts = 4;          // parameters.h:30
@@ -59,9 +57,8 @@ constexpr double threshCa34to7 = 0.0368369379834969;
 constexpr double threshCa56to8 = 0.00011447933531005;
 constexpr double threshMAX = 2.0, threshMAXCa = 0.0504410547074504;
 
-// a / b for the rate rows: FP64 on the integer pipe (correctly rounded, the
-// bits of a / b), FP32 as is
-__device__ __forceinline__ double fdiv(double a, double b) { return gw_div_rn(a, b); }
+// a / b for the rate rows (correctly rounded in FP64 and in FP32)
+__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float fdiv(float a, float b) { return a / b; }
 
 __device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
