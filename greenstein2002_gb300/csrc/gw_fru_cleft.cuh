@@ -258,7 +258,39 @@ struct StageCtx {
   uint32_t* my_hold_epoch;   // the epoch of this lane's FRU
   int f;                     // this lane's FRU (any value for a group without one)
   bool dirty;                // this FRU's staged words differ from its global row
+  int start;                 // words below this were not staged (stage_row)
+  const uint32_t* src;       // the global row the staging came from
 };
+
+// Stage an FRU's MT19937 row from `src` in shared memory: every word
+// (full), or only those from word mti on (rounded down to a 16-byte
+// boundary) -- the words its draws can reach before the row is next
+// regenerated.  Most FRUs do not reach word 624 within a stage, so this
+// copies about half a row on average instead of a whole one; a row that is
+// regenerated first gets its missing words (complete_row).
+__device__ __forceinline__ void stage_row(StageCtx& sc, const uint32_t* src, int mti, bool full, const Group& g) {
+  const int q0 = full ? 0 : (mti >> 2);
+  const uint4* s4 = reinterpret_cast<const uint4*>(src);
+  uint4* d4 = reinterpret_cast<uint4*>(sc.m);
+  for (int i = q0 + g.c; i < kMtN / 4; i += 4) d4[i] = s4[i];
+  sc.start = q0 * 4;
+  sc.src = src;
+  __syncwarp(g.mask);
+}
+
+// Before group l0/4's row is regenerated (or saved): the whole warp loads
+// the words that were not staged, from the row the staging came from
+// (unchanged in global memory until the FRU is stored).
+__device__ __forceinline__ void complete_row(StageCtx& sc, int lane, int l0, uint32_t* row) {
+  const int st = __shfl_sync(0xffffffffu, sc.start, l0);
+  if (st > 0) {
+    const uint4* s4 = reinterpret_cast<const uint4*>(__shfl_sync(0xffffffffu, (unsigned long long)sc.src, l0));
+    uint4* d4 = reinterpret_cast<uint4*>(row);
+    for (int i = lane; i < st / 4; i += 32) d4[i] = s4[i];
+    __syncwarp();
+    if ((lane >> 2) == (l0 >> 2)) sc.start = 0;
+  }
+}
 
 // The words of one substep are E_tot extra draws (lane c owns positions
 // pre .. pre+ne-1) followed by the 32 batch draws (lane c owns 8c .. 8c+7).
@@ -281,7 +313,7 @@ __device__ __forceinline__ void fetch_old(const StageCtx& sc, const Group& g, in
 
 // cross / copy: bit 4*i set when group i regenerates / first copies its
 // pre-regeneration words to its hold row in this epoch (lane 4*i's ballot).
-__device__ __forceinline__ void regen_crossing(const StageCtx& sc, int lane, unsigned cross, unsigned copy) {
+__device__ __forceinline__ void regen_crossing(StageCtx& sc, int lane, unsigned cross, unsigned copy) {
   while (cross) {
     const int l0 = __ffs(cross) - 1;
     cross &= cross - 1u;
@@ -289,6 +321,7 @@ __device__ __forceinline__ void regen_crossing(const StageCtx& sc, int lane, uns
     uint32_t* row = sc.rows + gi * kMtSmemStride;
     const int fg = __shfl_sync(0xffffffffu, sc.f, l0);  // the FRU of group gi
     __syncwarp();  // group gi has read its old words
+    complete_row(sc, lane, l0, row);
     if (copy & (1u << l0)) {
       const uint4* s4 = reinterpret_cast<const uint4*>(row);
       uint4* d4 = reinterpret_cast<uint4*>(sc.hold_base + (size_t)fg * kMtStride);
@@ -957,6 +990,8 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
   sc.f = f;
   sc.my_hold_epoch = s.hold_epoch + f;  // within the padded arrays even past the last FRU
   sc.dirty = false;
+  sc.start = 0;
+  sc.src = nullptr;
   bool restore = false;
   if (active) {
     if (p.flags & kFlagResume) {
@@ -984,7 +1019,7 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
   if (p.flags & kFlagAdvance) {
     // the FRUs' MT rows live in shared memory for the whole launch: every
     // draw and every regeneration is a shared-memory access
-    if (active) copy_row16(sc.m, restore ? hold : gm, g);
+    if (active) stage_row(sc, restore ? hold : gm, mti, restore, g);
     sc.dirty = restore;
     __syncwarp();
     advance4<R>(sc, g, active, cajsr, cass, w, mti, nsub, overflow);
@@ -1090,6 +1125,8 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
   sc.f = 0;
   sc.my_hold_epoch = s.hold_epoch;
   sc.dirty = false;
+  sc.start = 0;
+  sc.src = nullptr;
   Fru4<R> F;
   F.clk = {};
   F.jsr.set(0.0);
@@ -1144,7 +1181,7 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
       s.frus_s[(g.c + 1) * nf + ff] = F.ss.get();
       s.chan_s[g.c * nf + ff] = F.w;
     }
-    copy_row16(sc.m, restore ? s.mt_hold + (size_t)ff * kMtStride : s.mt + (size_t)ff * kMtStride, g);
+    stage_row(sc, restore ? s.mt_hold + (size_t)ff * kMtStride : s.mt + (size_t)ff * kMtStride, F.mti, restore, g);
     sc.dirty = restore;
     F.nsub = 0u;
     fru_begin(F, LS);

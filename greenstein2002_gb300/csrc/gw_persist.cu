@@ -334,6 +334,7 @@ __device__ __forceinline__ void regen_multi(cleft::StageCtx& sc, int lane, const
     uint32_t* hold_ep = (uint32_t*)__shfl_sync(kFull, (unsigned long long)sc.hold_epoch_base, l0);
     const uint32_t ep = __shfl_sync(kFull, epoch, l0);
     __syncwarp();  // the group has read its old words
+    cleft::complete_row(sc, lane, l0, row);
     if (copy_mask & (1u << l0)) {
       const uint4* s4 = reinterpret_cast<const uint4*>(row);
       uint4* d4 = reinterpret_cast<uint4*>(hold + (size_t)fg * kMtStride);
@@ -364,6 +365,8 @@ __device__ __forceinline__ void persist_body(const Args& a) {
   sc.my_hold_epoch = nullptr;
   sc.f = 0;
   sc.dirty = false;
+  sc.start = 0;
+  sc.src = nullptr;
   LaneStage<R> LS;
   Fru4<R> F;
   F.clk = {};
@@ -410,7 +413,7 @@ __device__ __forceinline__ void persist_body(const Args& a) {
       S->frus_s[(g.c + 1) * nf + ff] = F.ss.get();
       S->chan_s[g.c * nf + ff] = F.w;
     }
-    copy_row16(sc.m, restore ? S->mt_hold + (size_t)ff * kMtStride : S->mt + (size_t)ff * kMtStride, g);
+    stage_row(sc, restore ? S->mt_hold + (size_t)ff * kMtStride : S->mt + (size_t)ff * kMtStride, F.mti, restore, g);
     sc.dirty = restore;
     F.nsub = 0u;
     fru_begin(F, LS);
