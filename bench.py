@@ -73,9 +73,6 @@ REF_SAMPLE_MS = 3.0
 T975 = {1: 12.706, 2: 4.303, 3: 3.182, 4: 2.776, 5: 2.571, 6: 2.447, 7: 2.365, 8: 2.306, 9: 2.262, 10: 2.228,
         11: 2.201, 12: 2.179, 13: 2.160, 14: 2.145, 15: 2.131, 16: 2.120, 17: 2.110, 18: 2.101, 19: 2.093,
         20: 2.086, 24: 2.064, 30: 2.042, 40: 2.021, 63: 1.998, 127: 1.979, 255: 1.969}
-# algorithmic work per FRU-substep (static count of the reference's substep:
-# fru_rates_local + 2 x fcn_fru + simfru_local body, each add/mul/div/exp/
-# compare/convert counted once) and MT19937 bytes streamed per substep
 # DRAM bytes per stage launch of a 12,500-FRU cell, by kernel, from ncu's
 # dram__bytes_read + dram__bytes_write (profiles/): the fixed-layout FP64
 # kernel's 2,500-FRU plateau launch (6.67 MB, cold L2 per replay) times 5
@@ -83,7 +80,12 @@ T975 = {1: 12.706, 2: 4.303, 3: 3.182, 4: 2.776, 5: 2.571, 6: 2.447, 7: 2.365, 8
 TRAFFIC_PER_LAUNCH = {
     "fru_stage4_kernel": (5 * 6.672128e6, "ncu dram bytes of one 2,500-FRU plateau launch x 5 (cold L2 per replay; "
                                           "profiles/fru_stage4_kernel_plateau_2500fru.md)"),
+    "fru_stage4_packed_kernel": (3.3444e7, "ncu dram bytes of a 12,500-FRU cell's stage launches at 30 ms, mean of 3 "
+                                           "(profiles/fru_stage4_packed_kernel_plateau_12500fru_64perwarp.md)"),
 }
+# algorithmic work per FRU-substep (static count of the reference's substep:
+# fru_rates_local + 2 x fcn_fru + simfru_local body, each add/mul/div/exp/
+# compare/convert counted once) and MT19937 bytes streamed per substep
 FLOPS_PER_SUBSTEP = 700.0
 BYTES_PER_SUBSTEP = 384.0
 # GB300 FP32 (non-tensor) peak, nominal: 152 SMs x 128 FP32 lanes x 2 FLOP x 2.07 GHz
