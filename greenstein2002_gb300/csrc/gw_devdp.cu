@@ -239,15 +239,15 @@ extern "C" int gw_run_device(int n, gw_ctx** cells, const gw_settings* sets, dou
   }
   if (e == cudaSuccess) {
     void* kfun = prec == 1 ? (void*)gw::dp_round_kernel<float> : (void*)gw::dp_round_kernel<double>;
-    e = prec == 1 ? gw::stage_smem_attributes(gw::dp_round_kernel<float>)
-                  : gw::stage_smem_attributes(gw::dp_round_kernel<double>);
+    e = prec == 1 ? gw::stage_cache_attributes(gw::dp_round_kernel<float>)
+                  : gw::stage_cache_attributes(gw::dp_round_kernel<double>);
     void* kargs[] = {&args};
     cudaGraphNodeParams kp = {};
     kp.type = cudaGraphNodeTypeKernel;
     kp.kernel.func = kfun;
     kp.kernel.gridDim = dim3(acc);
     kp.kernel.blockDim = dim3(32 * warps);
-    kp.kernel.sharedMemBytes = warps * gw::kStageSmemPerWarp;
+    kp.kernel.sharedMemBytes = 0;
     kp.kernel.kernelParams = kargs;
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     if (e == cudaSuccess) e = cudaGraphAddNode(&knode, body, nullptr, nullptr, 0, &kp);

@@ -20,11 +20,17 @@
 //   - the four voltage exponentials of a substep are computed one per lane,
 //     and exp(2VF/RT) at the end of a substep is reused at the start of the
 //     next.
-// R = float: the mixed-precision method.  Transition rates and the local Ca
-// ODE are evaluated in FP32; FP64 is kept for the FRU Ca state itself (FP32
-// increments are accumulated in FP64), for the FRU clock and its step, and
-// for the cross-FRU flux sums.  Channel transitions use the complement form
-// 1 - u < dt*rate, which keeps full resolution near u = 1.
+// R = float: the mixed-precision method.  Transition rates, the local Ca ODE
+// and the FRU clock are evaluated in FP32, the Ca states and the clock
+// accumulated as compensated FP32 pairs; FP64 is kept for the FRU arrays in
+// memory and for the cross-FRU flux sums.  Channel transitions use the
+// complement form 1 - u < dt*rate, which keeps full resolution near u = 1.
+//
+// MT19937 rows are drawn from and regenerated in place, in the FRU's own
+// row in global memory (L1-cached; the kernels use no shared memory): on
+// GB300 this ran as fast as staging the eight rows of a warp in shared
+// memory for FP64 and 15% faster for mixed precision, whose warps the
+// staging's 20 KB per warp had held to eleven per SM.
 //
 // Reference: simfru_local.c:32-278, fru_rates_local.c:30-798, fcn_fru.c:23-137,
 // mt19937_local.c:97-240.
@@ -247,49 +253,24 @@ __device__ __forceinline__ void copy_row16(uint32_t* dst, const uint32_t* src, c
   __syncwarp(g.mask);
 }
 
-// The launch's view of one warp's 8 FRUs: their MT rows staged in shared
-// memory, and the global copy-on-twist rows of the first of them.
+// The launch's view of one warp's 8 FRUs: each lane's FRU row (in place,
+// global memory) and the copy-on-twist rows of the cell.
 struct StageCtx {
   const StageParams* p;
-  uint32_t* rows;            // 8 shared-memory rows, kMtSmemStride words apart
-  uint32_t* m;               // this lane's FRU row (one of rows)
-  uint32_t* hold_base;       // copy-on-twist rows of the cell (global), FRU-major
+  uint32_t* m;               // this lane's FRU row
+  uint32_t* hold_base;       // copy-on-twist rows of the cell, FRU-major
   uint32_t* hold_epoch_base; // their epochs
   uint32_t* my_hold_epoch;   // the epoch of this lane's FRU
   int f;                     // this lane's FRU (any value for a group without one)
-  bool dirty;                // this FRU's staged words differ from its global row
-  int start;                 // words below this were not staged (stage_row)
-  const uint32_t* src;       // the global row the staging came from
 };
 
-// Stage an FRU's MT19937 row from `src` in shared memory: every word
-// (full), or only those from word mti on (rounded down to a 16-byte
-// boundary) -- the words its draws can reach before the row is next
-// regenerated.  Most FRUs do not reach word 624 within a stage, so this
-// copies about half a row on average instead of a whole one; a row that is
-// regenerated first gets its missing words (complete_row).
-__device__ __forceinline__ void stage_row(StageCtx& sc, const uint32_t* src, int mti, bool full, const Group& g) {
-  const int q0 = full ? 0 : (mti >> 2);
-  const uint4* s4 = reinterpret_cast<const uint4*>(src);
-  uint4* d4 = reinterpret_cast<uint4*>(sc.m);
-  for (int i = q0 + g.c; i < kMtN / 4; i += 4) d4[i] = s4[i];
-  sc.start = q0 * 4;
-  sc.src = src;
-  __syncwarp(g.mask);
-}
-
-// Before group l0/4's row is regenerated (or saved): the whole warp loads
-// the words that were not staged, from the row the staging came from
-// (unchanged in global memory until the FRU is stored).
-__device__ __forceinline__ void complete_row(StageCtx& sc, int lane, int l0, uint32_t* row) {
-  const int st = __shfl_sync(0xffffffffu, sc.start, l0);
-  if (st > 0) {
-    const uint4* s4 = reinterpret_cast<const uint4*>(__shfl_sync(0xffffffffu, (unsigned long long)sc.src, l0));
-    uint4* d4 = reinterpret_cast<uint4*>(row);
-    for (int i = lane; i < st / 4; i += 32) d4[i] = s4[i];
-    __syncwarp();
-    if ((lane >> 2) == (l0 >> 2)) sc.start = 0;
-  }
+// Point the group at its FRU's row; on a resume whose epoch's snapshot
+// holds the row's words from before its last regeneration, put them back
+// first (send_resume_state's MT restore, mpi_slave.c:150-184).
+__device__ __forceinline__ void use_row(StageCtx& sc, uint32_t* row, const uint32_t* hold, bool restore,
+                                        const Group& g) {
+  if (restore) copy_row16(row, hold, g);
+  sc.m = row;
 }
 
 // The words of one substep are E_tot extra draws (lane c owns positions
@@ -313,15 +294,13 @@ __device__ __forceinline__ void fetch_old(const StageCtx& sc, const Group& g, in
 
 // cross / copy: bit 4*i set when group i regenerates / first copies its
 // pre-regeneration words to its hold row in this epoch (lane 4*i's ballot).
-__device__ __forceinline__ void regen_crossing(StageCtx& sc, int lane, unsigned cross, unsigned copy) {
+__device__ __forceinline__ void regen_crossing(const StageCtx& sc, int lane, unsigned cross, unsigned copy) {
   while (cross) {
     const int l0 = __ffs(cross) - 1;
     cross &= cross - 1u;
-    const int gi = l0 >> 2;
-    uint32_t* row = sc.rows + gi * kMtSmemStride;
-    const int fg = __shfl_sync(0xffffffffu, sc.f, l0);  // the FRU of group gi
-    __syncwarp();  // group gi has read its old words
-    complete_row(sc, lane, l0, row);
+    uint32_t* row = reinterpret_cast<uint32_t*>(__shfl_sync(0xffffffffu, (unsigned long long)sc.m, l0));
+    const int fg = __shfl_sync(0xffffffffu, sc.f, l0);  // the FRU of group l0/4
+    __syncwarp();  // the group has read its old words
     if (copy & (1u << l0)) {
       const uint4* s4 = reinterpret_cast<const uint4*>(row);
       uint4* d4 = reinterpret_cast<uint4*>(sc.hold_base + (size_t)fg * kMtStride);
@@ -806,13 +785,12 @@ __device__ __forceinline__ void substep_b(Fru4<R>& F, Sub4<R>& S, const LaneStag
 // Regenerate, with the whole warp, the MT rows whose draws in this substep
 // run past word 624 (`go`: this lane's FRU takes a substep now).
 template <typename R>
-__device__ __forceinline__ void regen_step(StageCtx& sc, int lane, const Group& g, bool go, const Fru4<R>& F,
+__device__ __forceinline__ void regen_step(const StageCtx& sc, int lane, const Group& g, bool go, const Fru4<R>& F,
                                            const Sub4<R>& S) {
   const bool cross = go && (F.mti + S.etot + 32 > kMtN);
   const unsigned cross_mask = __ballot_sync(0xffffffffu, cross && g.c == 0);
   const unsigned copy_mask = __ballot_sync(0xffffffffu, cross && g.c == 0 && *sc.my_hold_epoch != sc.p->epoch);
   if (cross_mask) regen_crossing(sc, lane, cross_mask, copy_mask);
-  if (cross) sc.dirty = true;
 }
 
 // One FRU over [t0, tf] by its four lanes (simfru_local.c:83-277).  cajsr and
@@ -951,7 +929,6 @@ __device__ __forceinline__ void avg_terms(int c, double jsr, double ss, uint32_t
 
 template <typename R, typename Fin>
 __device__ __forceinline__ void stage_body_fin(const DevState& s, const StageParams& p, int bidx, const Fin& fin) {
-  extern __shared__ __align__(16) uint32_t mt_stage[];  // [warps][8][kMtSmemStride]
   const int lane = threadIdx.x & 31;
   const int grp = bidx * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
   const int ngroups = (s.nfru + 7) >> 3;
@@ -983,15 +960,11 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
   uint32_t* gm = s.mt + (size_t)f * kMtStride;
   StageCtx sc;
   sc.p = &p;
-  sc.rows = mt_stage + (threadIdx.x >> 5) * 8 * kMtSmemStride;
-  sc.m = sc.rows + (lane >> 2) * kMtSmemStride;
+  sc.m = gm;
   sc.hold_base = s.mt_hold;
   sc.hold_epoch_base = s.hold_epoch;
   sc.f = f;
   sc.my_hold_epoch = s.hold_epoch + f;  // within the padded arrays even past the last FRU
-  sc.dirty = false;
-  sc.start = 0;
-  sc.src = nullptr;
   bool restore = false;
   if (active) {
     if (p.flags & kFlagResume) {
@@ -1017,14 +990,10 @@ __device__ __forceinline__ void stage_body_fin(const DevState& s, const StagePar
   }
   const uint32_t* hold = sc.hold_base + (size_t)f * kMtStride;
   if (p.flags & kFlagAdvance) {
-    // the FRUs' MT rows live in shared memory for the whole launch: every
-    // draw and every regeneration is a shared-memory access
-    if (active) stage_row(sc, restore ? hold : gm, mti, restore, g);
-    sc.dirty = restore;
+    if (active) use_row(sc, gm, hold, restore, g);
     __syncwarp();
     advance4<R>(sc, g, active, cajsr, cass, w, mti, nsub, overflow);
     __syncwarp();
-    if (active && sc.dirty) copy_row16(gm, sc.m, g);
   } else if (active && restore) {
     copy_row16(gm, hold, g);
   }
@@ -1097,7 +1066,6 @@ __device__ __forceinline__ void stage_body(const DevState& s, const StageParams&
 // non-advancing launch over the stored states, in the usual fixed order.
 template <typename R>
 __device__ __forceinline__ void stage_body_packed(const DevState& s, const StageParams& p, double* out) {
-  extern __shared__ __align__(16) uint32_t mt_stage[];  // [warps][8][kMtSmemStride]
   const int lane = threadIdx.x & 31;
   Group g;
   g.c = lane & 3;
@@ -1118,15 +1086,11 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
   lane_stage(p, g, LS);
   StageCtx sc;
   sc.p = &p;
-  sc.rows = mt_stage + (threadIdx.x >> 5) * 8 * kMtSmemStride;
-  sc.m = sc.rows + (lane >> 2) * kMtSmemStride;
+  sc.m = s.mt;
   sc.hold_base = s.mt_hold;
   sc.hold_epoch_base = s.hold_epoch;
   sc.f = 0;
   sc.my_hold_epoch = s.hold_epoch;
-  sc.dirty = false;
-  sc.start = 0;
-  sc.src = nullptr;
   Fru4<R> F;
   F.clk = {};
   F.jsr.set(0.0);
@@ -1181,13 +1145,11 @@ __device__ __forceinline__ void stage_body_packed(const DevState& s, const Stage
       s.frus_s[(g.c + 1) * nf + ff] = F.ss.get();
       s.chan_s[g.c * nf + ff] = F.w;
     }
-    stage_row(sc, restore ? s.mt_hold + (size_t)ff * kMtStride : s.mt + (size_t)ff * kMtStride, F.mti, restore, g);
-    sc.dirty = restore;
+    use_row(sc, s.mt + (size_t)ff * kMtStride, s.mt_hold + (size_t)ff * kMtStride, restore, g);
     F.nsub = 0u;
     fru_begin(F, LS);
   };
   auto finish = [&]() {
-    if (sc.dirty) copy_row16(s.mt + (size_t)f * kMtStride, sc.m, g);
     if (g.c == 0) {
       s.frus[f] = F.jsr.get();
       s.mti[f] = F.mti;

@@ -15,18 +15,18 @@ __global__ void __launch_bounds__(kMaxStageWarps * 32) fru_stage_mixed_kernel(De
 
 cudaError_t launch_stage_mixed(const DevState& s, const StageParams& p, int warps, cudaStream_t st) {
   const int blocks = stage_blocks(s.nfru, warps);
-  static const cudaError_t attr = stage_smem_attributes(fru_stage_mixed_kernel);
+  static const cudaError_t attr = stage_cache_attributes(fru_stage_mixed_kernel);
   if (attr != cudaSuccess) return attr;
-  fru_stage_mixed_kernel<<<blocks, 32 * warps, warps * kStageSmemPerWarp, st>>>(s, p);
+  fru_stage_mixed_kernel<<<blocks, 32 * warps, 0, st>>>(s, p);
   return cudaGetLastError();
 }
 
 __global__ void __launch_bounds__(kMaxStageWarps * 32) fru_stage_mixed_batch_kernel(BatchArgs a) { cleft::batch_body<float>(a); }
 
 cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, int warps, cudaStream_t st) {
-  static const cudaError_t attr = stage_smem_attributes(fru_stage_mixed_batch_kernel);
+  static const cudaError_t attr = stage_cache_attributes(fru_stage_mixed_batch_kernel);
   if (attr != cudaSuccess) return attr;
-  fru_stage_mixed_batch_kernel<<<nblocks, 32 * warps, warps * kStageSmemPerWarp, st>>>(a);
+  fru_stage_mixed_batch_kernel<<<nblocks, 32 * warps, 0, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -35,9 +35,9 @@ __global__ void __launch_bounds__(32) fru_stage_mixed_packed_kernel(DevState s, 
 }
 
 cudaError_t launch_stage_mixed_packed(const DevState& s, const StageParams& p, int warps, cudaStream_t st) {
-  static const cudaError_t attr = stage_smem_attributes(fru_stage_mixed_packed_kernel);
+  static const cudaError_t attr = stage_cache_attributes(fru_stage_mixed_packed_kernel);
   if (attr != cudaSuccess) return attr;
-  fru_stage_mixed_packed_kernel<<<warps, 32, kStageSmemPerWarp, st>>>(s, p);
+  fru_stage_mixed_packed_kernel<<<warps, 32, 0, st>>>(s, p);
   return cudaGetLastError();
 }
 

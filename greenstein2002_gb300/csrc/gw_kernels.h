@@ -12,21 +12,12 @@ constexpr int kStageThreads = 32;
 // Cleft-parallel stage kernels: 8 FRUs per warp, 1 .. kMaxStageWarps warps
 // per block (a launch-shape choice only: the results are the same bits).
 constexpr int kMaxStageWarps = 8;
-// Shared-memory staging of the 8 MT19937 rows of a warp, 624 words each
-// (2,496 B, a 16-byte multiple): 19,968 B per warp, so that eleven
-// single-warp blocks (with the 1 KB the runtime reserves per block) fit in
-// an SM's 228 KB -- enough to keep a 12,500-FRU cell's 1,563 warps resident
-// at once on 152 SMs.
-constexpr int kMtSmemStride = 624;
-constexpr int kStageSmemPerWarp = 8 * kMtSmemStride * 4;  // 19,968 B
-// Let a stage kernel take up to 8 warps' staging and prefer shared memory
-// over L1 in the SM's carveout.
+// The stage kernels use no shared memory: the FRUs' MT19937 rows are read
+// and regenerated in place in global memory, so the SM's unified on-chip
+// memory goes to L1, which holds the rows being drawn from.
 template <typename K>
-cudaError_t stage_smem_attributes(K kernel) {
-  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       kMaxStageWarps * kStageSmemPerWarp);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  return e;
+cudaError_t stage_cache_attributes(K kernel) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
 }
 inline int stage_blocks(int nfru, int warps) { return ((nfru + 7) / 8 + warps - 1) / warps; }
 // out[] slot of the device error flag (substep limit hit)

@@ -6,39 +6,39 @@
 // calls distrib_simFRU (mpi_master.c:369-469) five or six times per attempt,
 // and every call waits for the slowest FRU.  Here one resident grid serves
 // all cells at once.  Each cell's integrator posts one "operation" at a time
-// (a flux evaluation at an attempt's start, or an FRU stage over [t0, tf]);
-// an operation has two phases:
-//   FRU phase      (stages only) 4-lane groups of any warp take the cell's
-//                  FRUs one at a time from a per-cell counter, advance them
-//                  with the substep loop of the cleft kernels (advance4's
-//                  substep_a / substep_b, warp-wide MT19937 regeneration) and
-//                  store them;
-//   reduction      whole warps take chunks of 32 8-FRU groups and form each
-//                  group's flux (and output-average) partial sums exactly as
-//                  the fixed-layout stage kernel does -- same lanes, same
-//                  shuffle tree -- applying a pending save / resume for
-//                  operations that do not advance; the warp that finishes
-//                  the last chunk adds the partials in the fixed order of
-//                  cell_finish, forms the currents, runs the cell's
-//                  integrator step on the whole warp (dp_after_warp: the
-//                  arithmetic of gw_dp.c, the 37-state vectors split over
-//                  the lanes and fcn's exponentials one per lane) and posts
-//                  the cell's next operation.
-// A warp whose groups find nothing to take works on whatever else is open,
-// so one cell's slowest FRU no longer holds the GPU: other cells' FRUs fill
-// the idle lanes.  Every cell's arithmetic, reduction order and integrator
-// are those of its single-cell run, so its results are the same bits alone,
-// in any mix, and in the round-based device runner (gw_run_device).
+// (a flux evaluation at an attempt's start, or an FRU stage over [t0, tf]),
+// and warps take the operation's FRUs in batches of consecutive 8-FRU
+// groups from a per-cell counter.  A warp advances its batch's FRUs with the
+// substep loop of the cleft kernels (advance4's substep_a / substep_b,
+// warp-wide MT19937 regeneration), its eight 4-lane groups taking the
+// batch's FRUs one after another as they finish (the packed launches'
+// scheme, with a warp-uniform counter instead of a queue in memory); then
+// forms each group's flux (and output-average) partial sums exactly as the
+// fixed-layout stage kernel does -- same lanes, same shuffle tree -- from
+// the stored FRUs.  The warp that stores the operation's last batch adds
+// the partials in the fixed order of cell_finish, forms the currents, runs
+// the cell's integrator step on the whole warp (dp_after_warp: the
+// arithmetic of gw_dp.c, the 37-state vectors split over the lanes and
+// fcn's exponentials one per lane) and posts the cell's next operation.
+// Operations that do not advance (the flux at an attempt's start) take
+// their batches the same way and only apply a pending save / resume.
+// A warp that finds nothing in one cell works on whatever else is open, so
+// one cell's slowest FRU no longer holds the GPU.  Every cell's arithmetic,
+// reduction order and integrator are those of its single-cell run, so its
+// results are the same bits alone, in any mix, and in the round-based
+// device runner (gw_run_device).
 //
 // Waiting: a warp with nothing to do sleeps and checks a global progress
-// counter (FRUs and chunks finished); if it has not moved for `wait_ns`
-// (2 s by default; real operations take microseconds to milliseconds) the
-// kernel sets an error status and every warp returns, so the context stays
-// usable and the host reports the error.  No warp ever waits for a specific
-// other warp, so the grid needs no co-residency guarantee; it is sized to the
-// occupancy (one single-warp block per resident slot) all the same.
+// counter (batches and operations finished); if it has not moved for
+// `wait_ns` (2 s by default; real operations take microseconds to
+// milliseconds) the kernel sets an error status and every warp returns, so
+// the context stays usable and the host reports the error.  No warp ever
+// waits for a specific other warp, so the grid needs no co-residency
+// guarantee; it is sized to the occupancy (one single-warp block per
+// resident slot) all the same.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <new>
@@ -57,24 +57,20 @@ extern "C" int gw_internal_error(int code, const char* msg);
 namespace gw {
 namespace persist {
 
-constexpr int kChunkGroups = 32;  // 8-FRU groups per reduction chunk (256 FRUs)
-constexpr int kTakeFrus = 4;      // FRUs a 4-lane group takes at once (one counter update, one fence)
-constexpr int kMaxCells = 1024;   // cells of one run (16 mask words)
+constexpr int kMaxBatchGroups = 8;  // 8-FRU groups a warp takes at once, at most
+constexpr int kMaxCells = 1024;     // cells of one run (16 mask words)
 constexpr unsigned kFull = 0xffffffffu;
 enum : int { kStatusOk = 0, kStatusWatchdog = 3 };
 constexpr unsigned long long kDefaultWaitNs = 2000000000ull;
 
-// Scheduling state of one cell.  `take` and `red_take` are reset only when
-// their phase opens, so a warp that increments one of them late either gets
-// an index past the end (nothing to do) or a valid index of a phase that is
-// open, and it reads the operation's parameters after the increment.
+// Scheduling state of one cell.  `take` is reset only when an operation
+// opens, so a warp that increments it late either gets an index past the
+// end (nothing to do) or a valid batch of an open operation, and it reads
+// the operation's parameters after the increment.
 struct PCell {
-  unsigned long long take;  // next FRU of the open FRU phase (>= nfru: none)
-  unsigned done;            // FRUs of the open operation stored
-  unsigned red_take;        // next reduction chunk (>= nchunks: none)
-  unsigned red_done;        // reduction chunks finished
+  unsigned long long take;  // next 8-FRU group of the open operation (>= ngroups: none)
+  unsigned done;            // groups of the open operation stored and summed
   unsigned overflow;        // an FRU of the operation reached the substep limit
-  int nchunks;
   int finished;
 };
 
@@ -83,11 +79,11 @@ struct Args {
   DpCell* dp;
   PCell* pc;
   int ncells;
+  int batch;                     // 8-FRU groups per take (1 .. kMaxBatchGroups)
   unsigned* running;             // cells with output steps left
-  unsigned long long* fru_mask;  // bit per cell: its FRU phase has FRUs left to take
-  unsigned long long* red_mask;  // bit per cell: its reduction has chunks left to take
-  int nwords;                    // 64-bit words of each mask
-  unsigned long long* progress;  // FRUs and chunks finished
+  unsigned long long* open_mask; // bit per cell: its operation has groups left to take
+  int nwords;                    // 64-bit words of the mask
+  unsigned long long* progress;  // batches finished
   unsigned long long* ops;       // operations completed
   int* status;                   // kStatus*
   unsigned long long wait_ns;
@@ -99,24 +95,20 @@ __device__ __forceinline__ unsigned vload(const unsigned* p) { return *(const vo
 __device__ __forceinline__ unsigned long long vload(const unsigned long long* p) {
   return *(const volatile unsigned long long*)p;
 }
+__device__ __forceinline__ int ngroups_of(const DevState& s) { return (s.nfru + 7) >> 3; }
 
-// ---- posting operations (one thread) -----------------------------------------------
-// A cell's bit in a mask is set after its counter is reset (open), and the
-// warp that finds the counter exhausted clears the bit and then looks at the
-// counter again, setting the bit back if a new phase opened meanwhile; so a
-// phase with work left always has its bit set.
+// ---- the open-cell mask --------------------------------------------------------------
+// A cell's bit is set after its counter is reset (open), and the warp that
+// finds the counter exhausted clears the bit and then looks at the counter
+// again, setting the bit back if a new operation opened meanwhile; so an
+// operation with groups left always has its bit set.
 __device__ __forceinline__ void mask_set(unsigned long long* m, int ci) {
   atomicOr(&m[ci >> 6], 1ull << (ci & 63));
 }
-__device__ __forceinline__ void mask_clear_fru(const Args& a, int ci) {
-  atomicAnd(&a.fru_mask[ci >> 6], ~(1ull << (ci & 63)));
+__device__ __forceinline__ void mask_clear(const Args& a, int ci, int ngroups) {
+  atomicAnd(&a.open_mask[ci >> 6], ~(1ull << (ci & 63)));
   __threadfence();
-  if (vload(&a.pc[ci].take) < (unsigned long long)a.cells[ci].nfru) mask_set(a.fru_mask, ci);
-}
-__device__ __forceinline__ void mask_clear_red(const Args& a, int ci) {
-  atomicAnd(&a.red_mask[ci >> 6], ~(1ull << (ci & 63)));
-  __threadfence();
-  if (vload(&a.pc[ci].red_take) < (unsigned)a.pc[ci].nchunks) mask_set(a.red_mask, ci);
+  if (vload(&a.pc[ci].take) < (unsigned long long)ngroups) mask_set(a.open_mask, ci);
 }
 // a set bit of the mask at or after `from` (cyclically); -1: none
 __device__ __forceinline__ int mask_pick(const unsigned long long* m, int nwords, int ncells, int from) {
@@ -134,110 +126,25 @@ __device__ __forceinline__ int mask_pick(const unsigned long long* m, int nwords
   return -1;
 }
 
-static __device__ void open_reduction(const Args& a, int ci) {
-  PCell& pc = a.pc[ci];
-  pc.red_done = 0u;
-  atomicExch(&pc.red_take, 0u);
-  __threadfence();
-  mask_set(a.red_mask, ci);
-}
-
-// Post the operation dp_after has just set up in the cell's DpCell.
+// Post the operation dp_after has just set up in the cell's DpCell (one thread).
 static __device__ void post(const Args& a, int ci) {
   PCell& pc = a.pc[ci];
   pc.done = 0u;
   pc.overflow = 0u;
   __threadfence();
-  if (a.dp[ci].sp.flags & kFlagAdvance) {
-    atomicExch(&pc.take, 0ull);
-    __threadfence();
-    mask_set(a.fru_mask, ci);
-  } else {
-    open_reduction(a, ci);
-  }
-}
-
-// ---- reduction ---------------------------------------------------------------------
-// One 8-FRU group's partial sums into partials[grp * NV ..], by the whole
-// warp in the lanes of the fixed-layout kernel (FRU grp*8 + lane/4, cleft
-// lane%4): stage_body_fin's epilogue, with its save / resume handling for an
-// operation that does not advance.
-template <int NV>
-__device__ __forceinline__ void reduce_group(const DevState& s, const StageParams& p, int grp, const cleft::Group& g,
-                                             int lane) {
-  const int f = grp * 8 + (lane >> 2);
-  const bool active = f < s.nfru;
-  const size_t nf = (size_t)s.stride;
-  const bool apply = !(p.flags & kFlagAdvance);  // an advancing op applied them in its FRU phase
-  double cajsr = 0.0, cass = 0.0;
-  uint32_t w = 0u;
-  int mti = 0;
-  bool restore = false;
-  if (active) {
-    if (apply && (p.flags & kFlagResume)) {
-      cajsr = s.frus_s[f];
-      cass = s.frus_s[(g.c + 1) * nf + f];
-      w = s.chan_s[g.c * nf + f];
-      mti = s.mti_s[f];
-      restore = (s.hold_epoch[f] == p.epoch);
-    } else {
-      cajsr = __ldcg(&s.frus[f]);
-      cass = __ldcg(&s.frus[(g.c + 1) * nf + f]);
-      w = __ldcg(&s.chan[g.c * nf + f]);
-      mti = __ldcg(&s.mti[f]);
-    }
-    if (apply && (p.flags & kFlagSave)) {
-      if (g.c == 0) {
-        s.frus_s[f] = cajsr;
-        s.mti_s[f] = mti;
-      }
-      s.frus_s[(g.c + 1) * nf + f] = cass;
-      s.chan_s[g.c * nf + f] = w;
-    }
-  }
-  if (apply) {
-    if (active && restore) cleft::copy_row16(s.mt + (size_t)f * kMtStride, s.mt_hold + (size_t)f * kMtStride, g);
-    if (active) {
-      if (g.c == 0) {
-        s.frus[f] = cajsr;
-        s.mti[f] = mti;
-      }
-      s.frus[(g.c + 1) * nf + f] = cass;
-      s.chan[g.c * nf + f] = w;
-    }
-  }
-  double v[NV];
-#pragma unroll
-  for (int k = 0; k < NV; k++) v[k] = 0.0;
-  if (active) {
-    v[0] = cass;
-    v[1] = (g.c == 0) ? cajsr : 0.0;
-    if (lcc_open(w)) {
-      v[2] = cass;
-      v[3] = 1.0;
-    }
-    if (cl_of(w) == 2) v[4] = 1.0;
-  }
-  if (NV == 16) {
-    double t[11];
-    cleft::avg_terms(g.c, cajsr, cass, w, t);
-#pragma unroll
-    for (int k = 0; k < 11; k++) v[(5 + k) % NV] = active ? t[k] : 0.0;
-  }
-  cleft::warp_sum<NV>(v);
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < NV; k++) s.partials[grp * NV + k] = v[k];
+  atomicExch(&pc.take, 0ull);
+  __threadfence();
+  mask_set(a.open_mask, ci);
 }
 
 // The cell's totals from its group partials in cell_finish's order, the
 // currents, and the integrator step; then the next operation is posted (or
-// the cell is done).  Whole warp; the integrator runs on lane 0.
+// the cell is done).  Whole warp.
 template <int NV>
 __device__ __forceinline__ void finish_op(const Args& a, int ci, int lane) {
   const DevState& s = a.cells[ci];
   DpCell& c = a.dp[ci];
-  const int ngroups = (s.nfru + 7) >> 3;
+  const int ngroups = ngroups_of(s);
   __threadfence();
   double tot[NV];
 #pragma unroll
@@ -274,31 +181,219 @@ __device__ __forceinline__ void finish_op(const Args& a, int ci, int lane) {
   __syncwarp();
 }
 
-// Take and reduce one chunk of cell ci's open reduction; false if none left.
-static __device__ bool reduce_chunk(const Args& a, int ci, const cleft::Group& g, int lane) {
-  PCell& pc = a.pc[ci];
-  unsigned k = 0u;
-  if (lane == 0) {
-    k = atomicAdd(&pc.red_take, 1u);
-    if (k >= (unsigned)pc.nchunks - 1u) mask_clear_red(a, ci);
+// One 8-FRU group's partial sums into partials[grp * NV ..], by the whole
+// warp in the lanes of the fixed-layout kernel (FRU grp*8 + lane/4, cleft
+// lane%4), from the FRUs as stored: stage_body_fin's epilogue.
+template <int NV>
+__device__ __forceinline__ void group_partials(const DevState& s, int grp, const cleft::Group& g, int lane) {
+  const int f = grp * 8 + (lane >> 2);
+  const bool active = f < s.nfru;
+  const size_t nf = (size_t)s.stride;
+  double cajsr = 0.0, cass = 0.0;
+  uint32_t w = 0u;
+  if (active) {
+    cajsr = s.frus[f];
+    cass = s.frus[(g.c + 1) * nf + f];
+    w = s.chan[g.c * nf + f];
   }
-  k = __shfl_sync(kFull, k, 0);
-  if (k >= (unsigned)pc.nchunks) return false;
-  __threadfence();  // the operation's parameters and stored FRUs after the take
+  double v[NV];
+#pragma unroll
+  for (int k = 0; k < NV; k++) v[k] = 0.0;
+  if (active) {
+    v[0] = cass;
+    v[1] = (g.c == 0) ? cajsr : 0.0;
+    if (lcc_open(w)) {
+      v[2] = cass;
+      v[3] = 1.0;
+    }
+    if (cl_of(w) == 2) v[4] = 1.0;
+  }
+  if (NV == 16) {
+    double t[11];
+    cleft::avg_terms(g.c, cajsr, cass, w, t);
+#pragma unroll
+    for (int k = 0; k < 11; k++) v[(5 + k) % NV] = active ? t[k] : 0.0;
+  }
+  cleft::warp_sum<NV>(v);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; k++) s.partials[grp * NV + k] = v[k];
+}
+
+// One batch of cell ci's open operation: groups [grp0, grp0 + ng).  The
+// FRUs are loaded (applying the operation's save / resume), advanced when
+// the operation is a stage, and stored; then the groups' partial sums; the
+// warp that stores the operation's last batch finishes the operation.
+template <typename R>
+__device__ __forceinline__ void run_batch(const Args& a, int ci, int grp0, int ng, int lane) {
+  using namespace cleft;
   const DevState& s = a.cells[ci];
   const StageParams& p = a.dp[ci].sp;
-  const int ngroups = (s.nfru + 7) >> 3;
-  const int g1 = min(ngroups, (int)(k + 1u) * kChunkGroups);
-  const bool avg = (p.flags & kFlagAvg) != 0;
-  for (int grp = (int)k * kChunkGroups; grp < g1; grp++) {
-    if (avg) reduce_group<16>(s, p, grp, g, lane);
-    else reduce_group<5>(s, p, grp, g, lane);
+  const int n = s.nfru;
+  const int ngroups = ngroups_of(s);
+  const int f_begin = grp0 * 8;
+  const int f_end = min(n, (grp0 + ng) * 8);
+  const size_t nf = (size_t)s.stride;
+  const bool restore_op = (p.flags & kFlagResume) != 0;
+  Group g;
+  g.c = lane & 3;
+  g.base = lane & ~3;
+  g.mask = 0xfu << g.base;
+  bool overflow = false;
+  unsigned long long nsub_sum = 0ull;
+  if (p.flags & kFlagAdvance) {
+    LaneStage<R> LS;
+    lane_stage(p, g, LS);
+    StageCtx sc;
+    sc.p = &p;
+    sc.m = s.mt;
+    sc.hold_base = s.mt_hold;
+    sc.hold_epoch_base = s.hold_epoch;
+    sc.f = 0;
+    sc.my_hold_epoch = s.hold_epoch;
+    Fru4<R> F;
+    F.clk = {};
+    F.jsr.set(0.0);
+    F.ss.set(0.0);
+    F.w = 0u;
+    F.nsub = 0u;
+    F.mti = 0;
+    int f = -1;
+    auto load = [&](int ff) {
+      f = ff;
+      sc.f = ff;
+      sc.my_hold_epoch = s.hold_epoch + ff;
+      bool restore = false;
+      if (restore_op) {
+        F.jsr.set(s.frus_s[ff]);
+        F.ss.set(s.frus_s[(g.c + 1) * nf + ff]);
+        F.w = s.chan_s[g.c * nf + ff];
+        F.mti = s.mti_s[ff];
+        restore = (*sc.my_hold_epoch == p.epoch);
+      } else {
+        F.jsr.set(__ldcg(&s.frus[ff]));
+        F.ss.set(__ldcg(&s.frus[(g.c + 1) * nf + ff]));
+        F.w = __ldcg(&s.chan[g.c * nf + ff]);
+        F.mti = __ldcg(&s.mti[ff]);
+      }
+      if (p.flags & kFlagSave) {
+        if (g.c == 0) {
+          s.frus_s[ff] = F.jsr.get();
+          s.mti_s[ff] = F.mti;
+        }
+        s.frus_s[(g.c + 1) * nf + ff] = F.ss.get();
+        s.chan_s[g.c * nf + ff] = F.w;
+      }
+      use_row(sc, s.mt + (size_t)ff * kMtStride, s.mt_hold + (size_t)ff * kMtStride, restore, g);
+      F.nsub = 0u;
+      fru_begin(F, LS);
+    };
+    auto finish = [&]() {
+      if (g.c == 0) {
+        s.frus[f] = F.jsr.get();
+        s.mti[f] = F.mti;
+        nsub_sum += F.nsub;
+      }
+      s.frus[(g.c + 1) * nf + f] = F.ss.get();
+      s.chan[g.c * nf + f] = F.w;
+    };
+    // the batch's first eight FRUs one per group; then each group that
+    // stores its FRU takes the next, in group order (a warp-uniform count of
+    // the FRUs handed out, advanced by a ballot of the groups that need one)
+    int next = f_begin + 8;
+    {
+      const int ff = f_begin + (lane >> 2);
+      if (ff < f_end) load(ff);
+    }
+    __syncwarp();
+    while (true) {
+      const bool has = f >= 0;
+      bool go = has && F.clk.running(LS);
+      if (go && F.nsub >= (1u << 22)) {
+        overflow = true;
+        go = false;
+      }
+      if (!__any_sync(kFull, has)) break;
+      Sub4<R> S;
+      S.etot = 0;
+#pragma unroll
+      for (int i = 0; i < kRyR; i++) S.exw[i] = 0u;
+      S.p34 = R(0);
+      if (go) substep_a(F, S, LS, g, sc);
+      regen_step(sc, lane, g, go, F, S);
+      if (go) substep_b(F, S, LS, g, sc);
+      const bool stored = has && !(go && F.clk.running(LS));
+      if (stored) {
+        finish();
+        f = -1;
+      }
+      const unsigned need = __ballot_sync(kFull, stored && g.c == 0);
+      if (need) {
+        const int ff = next + __popc(need & ((1u << g.base) - 1u));
+        next += __popc(need);
+        if (stored && ff < f_end) load(ff);
+      }
+      __syncwarp();
+    }
+  } else {
+    // no advance: apply a pending save / resume (stage_body_fin without the
+    // substeps), in the fixed layout
+    for (int grp = grp0; grp < grp0 + ng; grp++) {
+      const int ff = grp * 8 + (lane >> 2);
+      if (ff < n) {
+        double cajsr, cass;
+        uint32_t w;
+        int mti;
+        bool restore = false;
+        if (restore_op) {
+          cajsr = s.frus_s[ff];
+          cass = s.frus_s[(g.c + 1) * nf + ff];
+          w = s.chan_s[g.c * nf + ff];
+          mti = s.mti_s[ff];
+          restore = (s.hold_epoch[ff] == p.epoch);
+        } else {
+          cajsr = __ldcg(&s.frus[ff]);
+          cass = __ldcg(&s.frus[(g.c + 1) * nf + ff]);
+          w = __ldcg(&s.chan[g.c * nf + ff]);
+          mti = __ldcg(&s.mti[ff]);
+        }
+        if (p.flags & kFlagSave) {
+          if (g.c == 0) {
+            s.frus_s[ff] = cajsr;
+            s.mti_s[ff] = mti;
+          }
+          s.frus_s[(g.c + 1) * nf + ff] = cass;
+          s.chan_s[g.c * nf + ff] = w;
+        }
+        if (restore) copy_row16(s.mt + (size_t)ff * kMtStride, s.mt_hold + (size_t)ff * kMtStride, g);
+        if (restore_op) {
+          if (g.c == 0) {
+            s.frus[ff] = cajsr;
+            s.mti[ff] = mti;
+          }
+          s.frus[(g.c + 1) * nf + ff] = cass;
+          s.chan[g.c * nf + ff] = w;
+        }
+      }
+    }
   }
+  __syncwarp();  // the stores above are visible to the whole warp
+  const bool avg = (p.flags & kFlagAvg) != 0;
+  for (int grp = grp0; grp < grp0 + ng; grp++) {
+    if (avg) group_partials<16>(s, grp, g, lane);
+    else group_partials<5>(s, grp, g, lane);
+  }
+  if (s.substeps) {
+    for (int o = 16; o > 0; o >>= 1) nsub_sum += __shfl_down_sync(kFull, nsub_sum, o);
+    if (lane == 0 && nsub_sum) atomicAdd(s.substeps, nsub_sum);
+  }
+  PCell& pc = a.pc[ci];
+  if (__any_sync(kFull, overflow) && lane == 0) atomicOr(&pc.overflow, 1u);
   __threadfence();
   __syncwarp();
   unsigned last = 0u;
   if (lane == 0) {
-    last = (atomicAdd(&pc.red_done, 1u) == (unsigned)pc.nchunks - 1u) ? 1u : 0u;
+    last = (atomicAdd(&pc.done, (unsigned)ng) + (unsigned)ng == (unsigned)ngroups) ? 1u : 0u;
     atomicAdd(a.progress, 1ull);
   }
   last = __shfl_sync(kFull, last, 0);
@@ -306,238 +401,53 @@ static __device__ bool reduce_chunk(const Args& a, int ci, const cleft::Group& g
     if (avg) finish_op<16>(a, ci, lane);
     else finish_op<5>(a, ci, lane);
   }
-  return true;
-}
-
-// A cell with reduction chunks left (warp-uniform; -1: none).
-static __device__ int find_reduction(const Args& a, int from, int lane) {
-  int ci = -1;
-  if (lane == 0) ci = mask_pick(a.red_mask, a.nwords, a.ncells, from);
-  return __shfl_sync(kFull, ci, 0);
-}
-
-// MT19937 regeneration of the rows whose draws run past word 624 in this
-// substep, by the whole warp (regen_step of the cleft kernels, with each
-// group's copy-on-twist target taken from its own cell).
-__device__ __forceinline__ void regen_multi(cleft::StageCtx& sc, int lane, const cleft::Group& g, bool go, int mti,
-                                            int etot, uint32_t epoch) {
-  const bool cross = go && (mti + etot + 32 > kMtN);
-  const unsigned cross_mask = __ballot_sync(kFull, cross && g.c == 0);
-  const unsigned copy_mask = __ballot_sync(kFull, cross && g.c == 0 && *sc.my_hold_epoch != epoch);
-  unsigned cm = cross_mask;
-  while (cm) {
-    const int l0 = __ffs(cm) - 1;
-    cm &= cm - 1u;
-    uint32_t* row = sc.rows + (l0 >> 2) * kMtSmemStride;
-    const int fg = __shfl_sync(kFull, sc.f, l0);
-    uint32_t* hold = (uint32_t*)__shfl_sync(kFull, (unsigned long long)sc.hold_base, l0);
-    uint32_t* hold_ep = (uint32_t*)__shfl_sync(kFull, (unsigned long long)sc.hold_epoch_base, l0);
-    const uint32_t ep = __shfl_sync(kFull, epoch, l0);
-    __syncwarp();  // the group has read its old words
-    cleft::complete_row(sc, lane, l0, row);
-    if (copy_mask & (1u << l0)) {
-      const uint4* s4 = reinterpret_cast<const uint4*>(row);
-      uint4* d4 = reinterpret_cast<uint4*>(hold + (size_t)fg * kMtStride);
-      for (int i = lane; i < kMtN / 4; i += 32) d4[i] = s4[i];
-      if (lane == 0) hold_ep[fg] = ep;
-    }
-    cleft::regen32(row, lane);
-  }
-  if (cross) sc.dirty = true;
 }
 
 template <typename R>
 __device__ __forceinline__ void persist_body(const Args& a) {
-  using namespace cleft;
-  extern __shared__ __align__(16) uint32_t mt_stage[];  // [8][kMtSmemStride] per warp
   const int lane = threadIdx.x & 31;
   const int warp = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  Group g;
-  g.c = lane & 3;
-  g.base = lane & ~3;
-  g.mask = 0xfu << g.base;
-  StageCtx sc;
-  sc.p = nullptr;
-  sc.rows = mt_stage + (threadIdx.x >> 5) * 8 * kMtSmemStride;
-  sc.m = sc.rows + (lane >> 2) * kMtSmemStride;
-  sc.hold_base = nullptr;
-  sc.hold_epoch_base = nullptr;
-  sc.my_hold_epoch = nullptr;
-  sc.f = 0;
-  sc.dirty = false;
-  sc.start = 0;
-  sc.src = nullptr;
-  LaneStage<R> LS;
-  Fru4<R> F;
-  F.clk = {};
-  F.jsr.set(0.0);
-  F.ss.set(0.0);
-  F.w = 0u;
-  F.nsub = 0u;
-  F.mti = 0;
-  LS.tf = 0.0;
-  LS.interval = 0.0;
-  int ci = -1, f = -1, f_end = -1, nfru = 0, taken = 0;
-  uint32_t epoch = 0u;
-  bool ovf = false;
-  const DevState* S = nullptr;
-  int cursor = (warp * 8 + (lane >> 2)) % a.ncells;
+  int cursor = warp % a.ncells;
   unsigned long long seen = 0ull, idle_since = 0ull;
   bool idle_clock = false;
-
-  // load FRU ff of the group's operation into the group's lanes
-  auto load = [&](int ff) {
-    const StageParams& p = a.dp[ci].sp;
-    f = ff;
-    sc.f = ff;
-    sc.my_hold_epoch = S->hold_epoch + ff;
-    const size_t nf = (size_t)S->stride;
-    bool restore = false;
-    if (p.flags & kFlagResume) {
-      F.jsr.set(S->frus_s[ff]);
-      F.ss.set(S->frus_s[(g.c + 1) * nf + ff]);
-      F.w = S->chan_s[g.c * nf + ff];
-      F.mti = S->mti_s[ff];
-      restore = (*sc.my_hold_epoch == epoch);
-    } else {
-      F.jsr.set(__ldcg(&S->frus[ff]));
-      F.ss.set(__ldcg(&S->frus[(g.c + 1) * nf + ff]));
-      F.w = __ldcg(&S->chan[g.c * nf + ff]);
-      F.mti = __ldcg(&S->mti[ff]);
-    }
-    if (p.flags & kFlagSave) {
-      if (g.c == 0) {
-        S->frus_s[ff] = F.jsr.get();
-        S->mti_s[ff] = F.mti;
-      }
-      S->frus_s[(g.c + 1) * nf + ff] = F.ss.get();
-      S->chan_s[g.c * nf + ff] = F.w;
-    }
-    stage_row(sc, restore ? S->mt_hold + (size_t)ff * kMtStride : S->mt + (size_t)ff * kMtStride, F.mti, restore, g);
-    sc.dirty = restore;
-    F.nsub = 0u;
-    fru_begin(F, LS);
-  };
-  // the next kTakeFrus FRUs of any open FRU phase (group-uniform; false: none)
-  auto take = [&]() -> bool {
-    int got_c = -1, got_f = -1;
-    if (g.c == 0) {
+  while (true) {
+    // the next batch of any open operation (lane 0 takes it for the warp)
+    int ci = -1, grp0 = 0, ng = 0;
+    if (lane == 0) {
       for (int tries = 0; tries < 4; tries++) {
-        const int cj = mask_pick(a.fru_mask, a.nwords, a.ncells, cursor);
+        const int cj = mask_pick(a.open_mask, a.nwords, a.ncells, cursor);
         if (cj < 0) break;
-        const unsigned n = (unsigned)a.cells[cj].nfru;
-        const unsigned idx = (unsigned)atomicAdd(&a.pc[cj].take, (unsigned long long)kTakeFrus);
-        if (idx + kTakeFrus >= n) mask_clear_fru(a, cj);  // the phase has no FRUs left to take
+        const int ngr = ngroups_of(a.cells[cj]);
+        const unsigned long long idx = atomicAdd(&a.pc[cj].take, (unsigned long long)a.batch);
+        if (idx + (unsigned long long)a.batch >= (unsigned long long)ngr) mask_clear(a, cj, ngr);
         cursor = cj;
-        if (idx >= n) continue;
-        got_c = cj;
-        got_f = (int)idx;
+        if (idx >= (unsigned long long)ngr) continue;
+        ci = cj;
+        grp0 = (int)idx;
+        ng = min(a.batch, ngr - grp0);
         break;
       }
     }
-    got_c = __shfl_sync(g.mask, got_c, g.base);
-    got_f = __shfl_sync(g.mask, got_f, g.base);
-    if (got_c < 0) return false;
-    __threadfence();  // the operation's parameters after the take
-    ci = got_c;
-    S = &a.cells[ci];
-    nfru = S->nfru;
-    f_end = min(nfru, got_f + kTakeFrus);
-    taken = f_end - got_f;
-    const StageParams& p = a.dp[ci].sp;
-    lane_stage(p, g, LS);
-    epoch = p.epoch;
-    sc.p = &p;
-    sc.hold_base = S->mt_hold;
-    sc.hold_epoch_base = S->hold_epoch;
-    ovf = false;
-    load(got_f);
-    return true;
-  };
-  // store the group's FRU and load the next one it holds; after its last,
-  // count them done -- the group that completes a phase opens the reduction
-  auto finish = [&]() {
-    const size_t nf = (size_t)S->stride;
-    if (sc.dirty) copy_row16(S->mt + (size_t)f * kMtStride, sc.m, g);
-    if (g.c == 0) {
-      S->frus[f] = F.jsr.get();
-      S->mti[f] = F.mti;
-      if (S->substeps) atomicAdd(S->substeps, (unsigned long long)F.nsub);
+    ci = __shfl_sync(kFull, ci, 0);
+    if (ci >= 0) {
+      grp0 = __shfl_sync(kFull, grp0, 0);
+      ng = __shfl_sync(kFull, ng, 0);
+      __threadfence();  // the operation's parameters after the take
+      run_batch<R>(a, ci, grp0, ng, lane);
+      idle_clock = false;
+      if (lane == 0) cursor = (cursor + 1) % a.ncells;  // spread the warps over the open cells
+      if (__shfl_sync(kFull, vload(a.status), 0) != kStatusOk) break;
+      continue;
     }
-    S->frus[(g.c + 1) * nf + f] = F.ss.get();
-    S->chan[g.c * nf + f] = F.w;
-    if (f + 1 < f_end) {
-      __syncwarp(g.mask);
-      load(f + 1);
-      return;
-    }
-    __threadfence();
-    __syncwarp(g.mask);
-    unsigned last = 0u;
-    if (g.c == 0) {
-      PCell& pc = a.pc[ci];
-      if (ovf) atomicOr(&pc.overflow, 1u);
-      last = (atomicAdd(&pc.done, (unsigned)taken) + (unsigned)taken == (unsigned)nfru) ? 1u : 0u;
-      if (last) {
-        __threadfence();
-        open_reduction(a, ci);
-      }
-      atomicAdd(a.progress, (unsigned long long)taken);
-    }
-    __syncwarp(g.mask);
-    ci = -1;
-    f = -1;
-  };
-
-  while (true) {
-    // flags for the end of this iteration, loaded now so that their latency
-    // hides behind the substep
     int st = kStatusOk;
-    unsigned run = 1u;
-    int red = 0;
+    unsigned run = 0u;
     if (lane == 0) {
       st = vload(a.status);
       run = vload(a.running);
-      for (int w = 0; w < a.nwords; w++) red |= vload(&a.red_mask[w]) != 0ull;
     }
-    bool worked = false;
-    // groups without an FRU take some
-    if (ci < 0) take();
-    const bool has = ci >= 0;
-    bool go = has && F.clk.running(LS);
-    if (go && F.nsub >= (1u << 22)) {
-      ovf = true;
-      go = false;
-    }
-    if (__any_sync(kFull, go)) {
-      Sub4<R> Sb;
-      Sb.etot = 0;
-#pragma unroll
-      for (int i = 0; i < kRyR; i++) Sb.exw[i] = 0u;
-      Sb.p34 = R(0);
-      if (go) substep_a(F, Sb, LS, g, sc);
-      regen_multi(sc, lane, g, go, F.mti, Sb.etot, epoch);
-      if (go) substep_b(F, Sb, LS, g, sc);
-      worked = true;
-    }
-    if (has && !(go && F.clk.running(LS))) {
-      finish();
-      worked = true;
-    }
-    __syncwarp();
     st = __shfl_sync(kFull, st, 0);
     run = __shfl_sync(kFull, run, 0);
-    if (st != kStatusOk) break;  // an error somewhere: every warp returns
-    if (run == 0u && !__any_sync(kFull, ci >= 0)) break;  // every cell is done
-    // reduction chunks: they are on a cell's critical path
-    if (__shfl_sync(kFull, red, 0)) {
-      const int rc = find_reduction(a, cursor, lane);
-      if (rc >= 0) worked = reduce_chunk(a, rc, g, lane) || worked;
-    }
-    if (__any_sync(kFull, worked)) {
-      idle_clock = false;
-      continue;
-    }
+    if (st != kStatusOk || run == 0u) break;  // an error somewhere, or every cell is done
     // nothing to do: sleep, and give up if nothing anywhere has progressed
     // for wait_ns
     int give_up = 0;
@@ -558,8 +468,7 @@ __device__ __forceinline__ void persist_body(const Args& a) {
   }
 }
 
-// Single-warp blocks: 191 registers and 19,968 B of MT staging per warp let
-// ten warps share an SM, as many as the packed stage kernels run.
+// Single-warp blocks, at least ten per SM (the register cap).
 __global__ void __launch_bounds__(32, 10) persist_kernel_fp64(Args a) { persist_body<double>(a); }
 __global__ void __launch_bounds__(32, 10) persist_kernel_mixed(Args a) { persist_body<float>(a); }
 
@@ -570,6 +479,20 @@ using gw::DpCell;
 using gw::persist::PCell;
 
 namespace {
+
+// 8-FRU groups a warp takes at once: up to four (32 FRUs, the packed
+// launches' best shape for full GPUs), fewer when the cells have too few
+// groups to give every resident warp two batches.  GW_PERSIST_GROUPS
+// (1..8) overrides the choice.
+int persist_batch(long long total_groups, long long warps) {
+  const char* env = getenv("GW_PERSIST_GROUPS");
+  if (env) {
+    const int v = atoi(env);
+    if (v >= 1 && v <= gw::persist::kMaxBatchGroups) return v;
+  }
+  long long b = warps > 0 ? total_groups / (2 * warps) : 1;
+  return (int)(b < 1 ? 1 : b > 4 ? 4 : b);
+}
 
 // One persistent run of n cells; wait_ns / release as in persist::Args.
 int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, double* states, double* oldsteps,
@@ -588,6 +511,7 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   std::vector<gw::DevState> hcells(n);
   std::vector<DpCell> hdp(n);
   std::vector<PCell> hpc(n);
+  long long total_groups = 0;
   for (int i = 0; i < n; i++) {
     gw_ctx* c = cells[i];
     cudaStreamSynchronize(c->stream);
@@ -623,16 +547,14 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
     d.sp.flags = c->pending;
     d.pending = 0;
     PCell& p = hpc[i];
-    memset(&p, 0, sizeof p);
-    p.take = (unsigned long long)c->d.nfru;  // no FRU phase open
-    p.nchunks = ((c->d.nfru + 7) / 8 + gw::persist::kChunkGroups - 1) / gw::persist::kChunkGroups;
-    p.red_take = 0u;                         // the first operation's reduction is open
+    memset(&p, 0, sizeof p);  // take = 0: the first operation (a flux) is open
+    total_groups += (c->d.nfru + 7) / 8;
   }
   const size_t ns = (size_t)n * n_steps;
   gw::DevState* dcells = nullptr;
   DpCell* ddp = nullptr;
   PCell* dpc = nullptr;
-  // counters: [0] running, [3] status, [4] release; then progress, ops; the two cell masks
+  // counters: [0] running, [3] status, [4] release; then progress, ops; the open-cell mask
   int* dcnt = nullptr;
   unsigned long long* dmask = nullptr;
   const int nwords = (n + 63) / 64;
@@ -645,12 +567,12 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   int rc = GW_OK;
   int dev = 0, sms = 0, per_sm = 0;
   const bool mixed = prec == 1;
-  const size_t smem = gw::kStageSmemPerWarp;
+  const size_t smem = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess)
-    e = mixed ? gw::stage_smem_attributes(gw::persist::persist_kernel_mixed)
-              : gw::stage_smem_attributes(gw::persist::persist_kernel_fp64);
+    e = mixed ? gw::stage_cache_attributes(gw::persist::persist_kernel_mixed)
+              : gw::stage_cache_attributes(gw::persist::persist_kernel_fp64);
   if (e == cudaSuccess)
     e = mixed ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gw::persist::persist_kernel_mixed, 32, smem)
               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gw::persist::persist_kernel_fp64, 32, smem);
@@ -660,7 +582,7 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   if (e == cudaSuccess) e = cudaMalloc(&ddp, sizeof(DpCell) * n);
   if (e == cudaSuccess) e = cudaMalloc(&dpc, sizeof(PCell) * n);
   if (e == cudaSuccess) e = cudaMalloc(&dcnt, sizeof(int) * 8);
-  if (e == cudaSuccess) e = cudaMalloc(&dmask, sizeof(unsigned long long) * 2 * nwords);
+  if (e == cudaSuccess) e = cudaMalloc(&dmask, sizeof(unsigned long long) * nwords);
   if (e == cudaSuccess) e = cudaMalloc(&d64, sizeof(unsigned long long) * 2);
   if (e == cudaSuccess) e = cudaMallocHost(&hout, sizeof(DpCell) * n);
   if (e == cudaSuccess && state_trace) e = cudaMalloc(&dst, sizeof(double) * ns * GW_NSTATE);
@@ -678,9 +600,9 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   if (e == cudaSuccess) e = cudaMemcpy(dpc, hpc.data(), sizeof(PCell) * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(dcnt, cnt, sizeof cnt, cudaMemcpyHostToDevice);
   {
-    // no FRU phase open; every cell's first operation (a flux) is in its reduction
-    std::vector<unsigned long long> m(2 * nwords, 0ull);
-    for (int i = 0; i < n; i++) m[nwords + (i >> 6)] |= 1ull << (i & 63);
+    // every cell's first operation (a flux) is open
+    std::vector<unsigned long long> m(nwords, 0ull);
+    for (int i = 0; i < n; i++) m[i >> 6] |= 1ull << (i & 63);
     if (e == cudaSuccess) e = cudaMemcpy(dmask, m.data(), sizeof(unsigned long long) * m.size(), cudaMemcpyHostToDevice);
   }
   if (e == cudaSuccess) e = cudaMemset(d64, 0, sizeof(unsigned long long) * 2);
@@ -690,9 +612,9 @@ int run_persistent(int n, gw_ctx** cells, const gw_settings* sets, double* t, do
   args.pc = dpc;
   args.ncells = n;
   args.running = (unsigned*)dcnt;
-  args.fru_mask = dmask;
-  args.red_mask = dmask + nwords;
+  args.open_mask = dmask;
   args.nwords = nwords;
+  args.batch = persist_batch(total_groups, (long long)sms * per_sm);
   args.status = dcnt + 3;
   args.release = hold ? dcnt + 4 : nullptr;
   args.progress = d64;

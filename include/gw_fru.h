@@ -256,12 +256,15 @@ int gw_run_device(int n, gw_ctx **cells, const gw_settings *sets, double *t, dou
 /* Persistent multi-cell kernel (the level-B seam of rk54pd, rk_pd54m.c:29, and
  * the stage dispatch of distrib_simFRU, mpi_master.c:369-469, for many cells
  * at once): n cells advance n_steps output steps each inside one resident
- * launch, captured with its copy-back as one CUDA graph.  Warps take FRUs,
- * reduction chunks and integrator steps from whichever cell has work, so no
- * cell waits for another's slowest FRU and no host thread or round trip sits
- * inside a step.  Arguments as gw_run_device; cells must share one precision
- * and not be in a batch.  A cell's results are the same bits alone, in any
- * mix and under gw_run_device.  If no work anywhere progresses for 2 s the
+ * launch, captured with its copy-back as one CUDA graph.  Warps take batches
+ * of 8-FRU groups (1 to 4 groups, fewer for small runs; the environment
+ * variable GW_PERSIST_GROUPS = 1..8 overrides) from whichever cell has an
+ * open stage or flux evaluation, advance and sum them, and the warp that
+ * finishes a cell's operation runs its integrator step; so no cell waits for
+ * another's slowest FRU and no host thread or round trip sits inside a step.
+ * Arguments as gw_run_device; cells must share one precision and not be in a
+ * batch.  A cell's results are the same bits alone, in any mix, for any batch
+ * size and under gw_run_device.  If no work anywhere progresses for 2 s the
  * launch ends with GW_ECUDA instead of waiting on. */
 int gw_run_persistent(int n, gw_ctx **cells, const gw_settings *sets, double *t, double *states, double *oldsteps,
                       int n_steps, double *state_trace, double *other_trace, double *cur_trace);

@@ -6,8 +6,9 @@ flux reductions and Dormand-Prince steps inside one resident launch.
   bits for every cell (global states, traces, FRU state and MT19937 words),
   in FP64 and in mixed precision, with cells of uneven FRU count, pacing
   cycle length and conductance scales.
-- A cell's result is the same alone and in the mix, and the same whether a
-  run is made in one call or split into several.
+- A cell's result is the same alone and in the mix, whatever the number of
+  8-FRU groups a warp takes at once, and the same whether a run is made in
+  one call or split into several.
 - The wait limit: when a flag that nothing sets holds a cell's next
   operation, every warp gives up after the limit and the launch returns an
   error status; the context stays usable."""
@@ -56,6 +57,18 @@ def test_persistent_matches_round_runner(gw, prec):
     per = _run(gw, SIZES, prec, steps, persistent=True, scales=SCALES)
     _same(dev, per)
     assert np.all(per[1] == steps)
+
+
+@pytest.mark.parametrize("groups", ["3", "8"])
+def test_persistent_batch_sizes_same_bits(gw, groups, monkeypatch):
+    """Warps taking 3 or 8 groups of 8 FRUs at a time (partial batches at
+    every cell's end, groups taking the batch's FRUs as they finish) give
+    the round runner's bits."""
+    steps = 8
+    dev = _run(gw, SIZES, "fp64", steps, persistent=False, scales=SCALES)
+    monkeypatch.setenv("GW_PERSIST_GROUPS", groups)
+    per = _run(gw, SIZES, "fp64", steps, persistent=True, scales=SCALES)
+    _same(dev, per)
 
 
 def test_persistent_same_alone_and_in_the_mix(gw):
