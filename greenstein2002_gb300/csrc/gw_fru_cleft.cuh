@@ -128,12 +128,16 @@ __device__ __forceinline__ bool leave_ge(uint32_t y, double dt, double R) {
   thresh(P, fl, ex);
   return (uint64_t)y > fl || (ex && (uint64_t)y == fl);
 }
+// 2^32 - y rounded to FP32, from a 32-bit conversion (0 - y wraps to it for
+// y > 0): the same value as converting the 33-bit integer, without a 64-bit
+// integer conversion, which runs on the FP64 pipe.
+__device__ __forceinline__ float comp_u32(uint32_t y) { return y ? (float)(0u - y) : 4294967296.0f; }
 // FP32: complement form, 1 - u = (2^32 - y)/2^32 against dt*R
 __device__ __forceinline__ bool leave_gt(uint32_t y, float dt, float R) {
-  return (float)(4294967296ull - (uint64_t)y) < dt * R * 4294967296.0f;
+  return comp_u32(y) < dt * R * 4294967296.0f;
 }
 __device__ __forceinline__ bool leave_ge(uint32_t y, float dt, float R) {
-  return (float)(4294967296ull - (uint64_t)y) <= dt * R * 4294967296.0f;
+  return comp_u32(y) <= dt * R * 4294967296.0f;
 }
 
 // Destination of a channel that leaves its state (simfru_local.c:215-253):
@@ -144,7 +148,7 @@ __device__ __forceinline__ int choose_dest(const double r[4], const int d[4], in
   return pick_dest(r, d, len, dt, (double)y / 4294967296.0);
 }
 __device__ __forceinline__ int choose_dest(const float r[4], const int d[4], int len, float dt, uint32_t y) {
-  const float c = (float)(4294967296ull - (uint64_t)y) * 2.3283064365386963e-10f;
+  const float c = comp_u32(y) * 2.3283064365386963e-10f;
   float rem = dt * r[0] - dt * r[1];
   int n = 1;
   while (c < rem && n + 1 < len) {
