@@ -80,8 +80,9 @@ T975 = {1: 12.706, 2: 4.303, 3: 3.182, 4: 2.776, 5: 2.571, 6: 2.447, 7: 2.365, 8
 TRAFFIC_PER_LAUNCH = {
     "fru_stage4_kernel": (5 * 6.672128e6, "ncu dram bytes of one 2,500-FRU plateau launch x 5 (cold L2 per replay; "
                                           "profiles/fru_stage4_kernel_plateau_2500fru.md)"),
-    "fru_stage4_packed_kernel": (3.3444e7, "ncu dram bytes of a 12,500-FRU cell's stage launches at 30 ms, mean of 3 "
-                                           "(profiles/fru_stage4_packed_kernel_plateau_12500fru_64perwarp.md)"),
+    "fru_stage4_packed_kernel": (4.18e7, "ncu dram bytes of two stage launches of a 50,000-FRU cell at 30 ms with the "
+                                         "SMs full, mean, / 4 (the bytes are per FRU: its state and MT row; "
+                                         "profiles/fru_stage4_packed_kernel_saturated_50000fru_32perwarp.md)"),
 }
 # algorithmic work per FRU-substep (static count of the reference's substep:
 # fru_rates_local + 2 x fcn_fru + simfru_local body, each add/mul/div/exp/
@@ -1020,7 +1021,10 @@ def run_gpu(args, dist):
         for r in serving["sweep"]:
             r["speedup_12500_equiv_vs_fp64_one_cell"] = r["cell_ms_per_s_12500_equiv"] / one["value"]
     e2e = ens.get("e2e")
-    full_cell = time_full_cell(args) if args.full_cell and dist.world == 1 else None
+    full_cell = (time_full_cell(args) if args.full_cell and dist.world == 1 else
+                 {"run": False, "enable": "--full-cell",
+                  "why": "one cell's whole protocol (5,300 simulated ms) in FP64 and in mixed precision takes "
+                         "about 8.5 minutes of wall time, longer than the rest of this line together"})
 
     # ---- CPU baseline: the reference program on one host core ----
     cpu = None
