@@ -151,6 +151,9 @@ def parse():
                     help="Poisson arrival rates (req/s) of the serving sweep")
     ap.add_argument("--serve-requests", type=int, default=16,
                     help="requests per rate (at most rate x 24 s of arrivals, at least 16)")
+    ap.add_argument("--serve-baseline", action="store_true",
+                    help="also run the serving section's request list in FP64 one request at a time (the "
+                         "like-for-like denominator of the serving throughput)")
     ap.add_argument("--serve-ms", type=float, default=1000.0,
                     help="cap on each request's simulated ms: the default 1000 keeps the clamp run whole and the "
                          "first second of a paced one; 0 runs every request's whole protocol (1-10 beats, minutes)")
@@ -805,6 +808,25 @@ def time_serving(G, args, rate):
                              "allocations_while_serving": st["allocs"] - allocs0}}
 
 
+def time_serving_fp64_sequential(G, args, rate):
+    """The serving denominator: the same request list (the same seed, so the
+    same sizes, protocols and durations as time_serving at `rate`) run in FP64
+    one request at a time, each submitted when the previous one is done."""
+    reqs, _ = serve_requests(G, args, rate)
+    srv = G.Server("fp64", slots=1, mem_budget_bytes=int(args.serve_budget_gb * (1 << 30)), lockstep=False)
+    for size in sorted(set(r.nfru for r in reqs)):
+        srv.reserve(size, 1)
+    t0 = time.perf_counter()
+    for r in reqs:
+        srv.submit(r)
+    srv.wait()
+    wall = time.perf_counter() - t0
+    srv.close()
+    cell_ms = sum(r.duration_ms for r in reqs)
+    return {"requests": len(reqs), "ok": all(r.status == 0 for r in reqs), "simulated_ms": cell_ms, "wall_s": wall,
+            "cell_ms_per_s": cell_ms / wall, "precision": "fp64", "slots": 1}
+
+
 def caf_run(settings, workdir):
     """Run the C host driver (gw_caf, the reference program's main loop over
     libgw_fru.so) with key=value settings; returns (wall s, states,
@@ -1020,6 +1042,14 @@ def run_gpu(args, dist):
                    "sweep": [time_serving(G, args, r) for r in args.serve_rates]}
         for r in serving["sweep"]:
             r["speedup_12500_equiv_vs_fp64_one_cell"] = r["cell_ms_per_s_12500_equiv"] / one["value"]
+        if args.serve_baseline:
+            base = time_serving_fp64_sequential(G, args, args.serve_rates[0])
+            base["speedup_of_serving"] = serving["sweep"][0]["cell_ms_per_s"] / base["cell_ms_per_s"]
+            serving["fp64_one_at_a_time"] = base
+        else:
+            serving["fp64_one_at_a_time"] = {"run": False, "enable": "--serve-baseline",
+                                             "why": "the same request list in FP64, one request at a time, takes "
+                                                    "several minutes"}
     e2e = ens.get("e2e")
     full_cell = (time_full_cell(args) if args.full_cell and dist.world == 1 else
                  {"run": False, "enable": "--full-cell",

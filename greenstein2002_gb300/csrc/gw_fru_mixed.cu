@@ -30,7 +30,7 @@ cudaError_t launch_stage_mixed_batch(const BatchArgs& a, int nblocks, int warps,
   return cudaGetLastError();
 }
 
-__global__ void __launch_bounds__(32) fru_stage_mixed_packed_kernel(DevState s, StageParams p) {
+__global__ void __launch_bounds__(32, 16) fru_stage_mixed_packed_kernel(DevState s, StageParams p) {
   cleft::stage_body_packed<float>(s, p, s.out);
 }
 

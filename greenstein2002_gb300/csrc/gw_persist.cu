@@ -470,7 +470,7 @@ __device__ __forceinline__ void persist_body(const Args& a) {
 
 // Single-warp blocks, at least ten per SM (the register cap).
 __global__ void __launch_bounds__(32, 10) persist_kernel_fp64(Args a) { persist_body<double>(a); }
-__global__ void __launch_bounds__(32, 16) persist_kernel_mixed(Args a) { persist_body<float>(a); }
+__global__ void __launch_bounds__(32, 10) persist_kernel_mixed(Args a) { persist_body<float>(a); }
 
 }  // namespace persist
 }  // namespace gw
