@@ -26,7 +26,9 @@ the FP64 ensemble: peak Cai with a 95% interval, ensemble-mean V, JSR
 depletion, open probabilities), one cell alone ("one_cell", "mixed"), a
 batched run ("batched": 64 cells of NFRU 1250-12,500 with varied pacing and
 conductances, mixed precision) and a serving sweep ("serving": Poisson
-arrivals of cell requests, p50/p99 latency).  Before each timed section the
+arrivals of cell requests, p50/p99 latency; with --serve-baseline also the
+same request list in FP64 one request at a time, its like-for-like
+denominator).  Before each timed section the
 launch-shape autotuner picks lanes per FRU and warps per block on the
 section's own workload ("tuning"; results do not depend on the choice), and
 `roofline.kernel` names the stage kernel it picked.
