@@ -1,4 +1,4 @@
-"""Build the reference (mwalker174/greenstein2002) serially, for use as a checker.
+"""Build the reference (mwalker174/greenstein2002) serially, to check the GPU path against.
 
 Test infrastructure only: nothing in the product imports or links what this
 script builds.
