@@ -41,7 +41,6 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include <new>
 #include <string>
 #include <vector>
 
