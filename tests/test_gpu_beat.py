@@ -4,7 +4,7 @@ sequences and end in identical channel states for at least 99% of FRUs, and
 the global traces agree.  Every launch shape the FP64 path ships is run:
 one thread per FRU, four lanes per FRU (8 FRUs per warp), and the packed
 launches the autotuner picks for the FP64 ensemble (4-lane groups taking
-FRUs from a queue, 64 FRUs per warp on average)."""
+FRUs from a queue, 32 FRUs per warp on average)."""
 import zlib
 
 import numpy as np
@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 # (lanes per FRU, packed FRUs per warp; 0 = the fixed layout)
-SHAPES = {"1_lane": (1, 0), "4_lanes": (4, 0), "packed_64_fru_per_warp": (4, 64)}
+SHAPES = {"1_lane": (1, 0), "4_lanes": (4, 0), "packed_32_fru_per_warp": (4, 32)}
 
 
 @pytest.mark.parametrize("shape", sorted(SHAPES))
