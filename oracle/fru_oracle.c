@@ -372,6 +372,11 @@ static int pick(const exit_row *e, double dt, double u, int cur)
     return e->dest[n];
 }
 
+/* FRU-substeps taken by orc_simfru since the library was loaded (the
+ * workload unit; the CPU stand-in of the native API reports it). */
+static unsigned long long orc_substeps_total = 0;
+unsigned long long orc_substep_count(void) { return orc_substeps_total; }
+
 void orc_simfru(double t0, double tf, const double dep0[3], const double depf[3], int ltype[NCLEFT][2],
                 int ryr[NCLEFT][NRYR], int ito2[NCLEFT], double frus[5], int *mti, uint32_t mt[MTN])
 {
@@ -386,6 +391,7 @@ void orc_simfru(double t0, double tf, const double dep0[3], const double depf[3]
         for (i = 0; i < NRYR; i++) nopen[c] += ryr_open(ryr[c][i]);
     }
     while (t < tf) {
+        orc_substeps_total++;
         mx = fru_tables_eval(&T, ltype, ryr, ito2, dep[0], frus, mti, mt);
         /* substep size, :135-146 */
         dt = DMIN(0.1 / mx, 10.001e-3);

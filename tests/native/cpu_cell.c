@@ -19,6 +19,7 @@ void orc_simfru_batch(int n, double t0, double tf, const double dep0[3], const d
 void orc_flux_sums(int n, const int *ltype, const int *ito2, const double *frus, double num[5]);
 void orc_avg_sums(int n, const int *ltype, const int *ryr, const int *ito2, const double *frus, double num[11]);
 void orc_currents(int nfru, double scale, const double dep[3], const double num[5], double out[4]);
+unsigned long long orc_substep_count(void);
 
 typedef struct {
     double *frus; int *ltype, *ryr, *ito2, *mti; uint32_t *mt;
@@ -118,7 +119,15 @@ int gw_stage(gw_ctx *c, double t0, double tf, const double dep0[3], const double
 {
     double nm[5];
     set_t *s = &c->live;
+    static int nstage = 0;
+    const unsigned long long before = orc_substep_count();
     orc_simfru_batch(c->n, t0, tf, dep0, depf, s->ltype, s->ryr, s->ito2, s->frus, s->mti, s->mt);
+    c->substeps += orc_substep_count() - before;
+    /* GW_CPU_STAGE_LOG: one line per stage with its FRU-substeps, to pair
+     * the stage launches of a GPU profile with their workload */
+    if (getenv("GW_CPU_STAGE_LOG"))
+        fprintf(stderr, "stage %d [%.6f, %.6f] FRU-substeps %llu\n", ++nstage, t0, tf,
+                orc_substep_count() - before);
     orc_flux_sums(c->n, s->ltype, s->ito2, s->frus, nm);
     if (out) orc_currents(c->n, c->scale, depf, nm, out);
     if (num) memcpy(num, nm, sizeof nm);
